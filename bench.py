@@ -1,0 +1,353 @@
+"""Benchmark of the pair-detection path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--workload NAME]
+
+A step is one self-intersection query over the whole workload (count, scan,
+scatter, pair test, compaction; the autotuner's choice is memoised after the
+first query of a context). Default workload: 4,194,304 3-D boxes drawn from a
+mixture of 64 Gaussians (sigma 0.02, means U[0.1,0.9]^3), lognormal sides
+(median 0.002, log-sigma 0.5), fp32 quantised to the PBIG API's unsigned
+coordinates (range 2^24); synthetic, seeded, generated on the host.
+
+Reported: ``value`` = boxes/s with the boxes resident in HBM (CUDA events on
+the query stream, L2 flushed between steps); ``e2e`` = the same through the
+C ABI with pinned host buffers (H2D of the boxes and D2H of every pair inside
+the timed region, host wall clock); ``roofline`` for the kernel with the
+largest share of device time; ``cpu_baseline`` = the oracle (CPU restatement
+of the reference pipeline, all host threads) on a bounded sample.
+
+With --gpus N under torchrun every rank runs an independent replica on its
+own GPU (the single-scene path does not shard); value = all ranks' boxes /
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "overlap pairs/s & boxes/s at 4M 3D boxes"
+UNIT = "boxes/s"
+BOX_BYTES = 28  # RectInfo, 3-D
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload(name: str):
+    from pbig_gb300 import gen
+    if name == "clustered4m":
+        return gen.clustered3d(4194304, seed=0), gen.RANGE, "3D self-intersection, 4,194,304 boxes, 64-Gaussian mixture (sigma 0.02), lognormal sides (median 0.002, log-sigma 0.5), seed 0"
+    if name == "plain2d":
+        return gen.uniform2d(65536, seed=0), gen.RANGE, "2D self-intersection, 65,536 boxes, uniform corners, sides U[0.001,0.005], seed 0"
+    raise SystemExit(f"unknown workload {name}")
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def algorithmic_bytes(st: dict, n: int) -> dict:
+    """Bytes each kernel must move at minimum (per launch): boxes are read
+    whole (28 B), cells as one u32 count/start, entries as one u32, pairs as
+    two u32; the pair test reads each entry and its box coordinates once."""
+    C, E, P = st["cells"], st["entries"], st["pairs"]
+    return {
+        "count": n * BOX_BYTES + C * 4,
+        "scan": 2 * C * 4,
+        "scatter": n * BOX_BYTES + C * 4 + E * 4,
+        "pairs": E * (4 + 24) + 8 * P,
+    }
+
+
+def cpu_baseline(boxes, range_, budget_s: float, threads: int):
+    """Oracle (reference pipeline restated on the CPU, reference cell-size
+    heuristic, all host threads) on the first n' boxes, n' sized so that one
+    run takes about budget_s seconds."""
+    from oracle import oracle as O
+    n = len(boxes)
+    frac = 1 / 64
+    m = max(1024, int(n * frac))
+    t0 = time.perf_counter()
+    O.grid_pairs(boxes[:m], range_, count_only=True, threads=threads)
+    dt = time.perf_counter() - t0
+    # the reference heuristic keeps the work per box roughly proportional to
+    # the density, so time grows ~ n'^2 at fixed domain: scale conservatively
+    while m < n and dt < budget_s / 4:
+        m = min(n, m * 2)
+        t0 = time.perf_counter()
+        _, st = O.grid_pairs(boxes[:m], range_, count_only=True, threads=threads)
+        dt = time.perf_counter() - t0
+    _, st = O.grid_pairs(boxes[:m], range_, count_only=True, threads=threads)
+    t0 = time.perf_counter()
+    _, st = O.grid_pairs(boxes[:m], range_, count_only=True, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": m / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {m} of {n} boxes (same generator), oracle grid pipeline with the reference cell-size heuristic (cs={st['cs']}), {st['pairs']} pairs, {dt:.2f} s",
+            "pairs_per_s": st["pairs"] / dt}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        rank = int(os.environ["RANK"])
+        local = int(os.environ.get("LOCAL_RANK", rank))
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        return rank, local, ws
+    return 0, 0, 1
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, rank, ws):
+    """Reference arm: the reference has no CPU implementation of its own, so
+    its CPU path is the oracle's restatement of its pipeline (reference cell
+    heuristic), timed on the host cores with all threads."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    boxes, rng, desc = workload(args.workload)
+    threads = os.cpu_count() or 1
+    total_budget = 150.0
+    per_step = total_budget / max(1, args.steps + args.warmup)
+    n = len(boxes)
+    m = max(1024, n // 64)
+    while m < n:
+        t0 = time.perf_counter()
+        O.grid_pairs(boxes[:m], rng, count_only=True, threads=threads)
+        if time.perf_counter() - t0 > per_step / 3:
+            break
+        m = min(n, m * 2)
+    sample = boxes[:m]
+    for _ in range(args.warmup):
+        O.grid_pairs(sample, rng, count_only=True, threads=threads)
+    ts = []
+    st = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, st = O.grid_pairs(sample, rng, count_only=True, threads=threads)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.mean(ts))
+    val = m / t
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": desc, "sample_boxes": m, "parallelism": "cpu threads"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"first {m} of {n} boxes per step; oracle restatement of the reference grid pipeline with its cell-size heuristic (cs={st['cs']}); {st['pairs']} pairs per step"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "pairs_per_s": st["pairs"] / t}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank, local, ws):
+    import torch
+    from pbig_gb300 import Engine
+
+    torch.cuda.set_device(local)
+    boxes, rng, desc = workload(args.workload)
+    n = len(boxes)
+    dev = torch.from_numpy(boxes.view(np.int32)).to(f"cuda:{local}")
+    host = torch.from_numpy(boxes.view(np.int32)).pin_memory()
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")  # > L2 (129 MB)
+    eng = Engine(local)
+
+    for _ in range(args.warmup):
+        eng.self_intersect(dev, rng, stream=stream)
+        torch.cuda.synchronize()
+    P = eng.result_count()
+    out_host = torch.empty((P, 2), dtype=torch.int32).pin_memory()
+
+    # device-resident timing
+    step_ms, phase_acc, kernels = [], {}, 0
+    stats = None
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            np_ = eng.self_intersect(dev, rng, stream=stream)
+            b.record(stream)
+            b.synchronize()
+            step_ms.append(a.elapsed_time(b))
+            stats = eng.stats()
+            kernels += stats["kernels"]
+            for k, v in stats["phase_ms"].items():
+                phase_acc[k] = phase_acc.get(k, 0.0) + v
+            assert np_ == P
+        torch.cuda.synchronize()
+    barrier(ws)
+    t_step = allmax(float(np.sum(step_ms)) / 1e3, ws)
+    value = n * args.steps * ws / t_step
+    phase = {k: v / args.steps for k, v in phase_acc.items()}
+
+    # end to end through the C ABI with pinned host buffers
+    e2e_t = []
+    for i in range(max(2, args.steps // 2) + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.self_intersect(host, rng, stream=stream)
+        eng.pairs_into(out_host, stream=stream)
+        eng.sync(stream)
+        t1 = time.perf_counter()
+        if i > 0:
+            e2e_t.append(t1 - t0)
+    e2e_step = allmax(float(np.mean(e2e_t)), ws)
+    e2e = {"value": n * ws / e2e_step, "unit": UNIT, "h2d_bytes_per_step": n * BOX_BYTES,
+           "d2h_bytes_per_step": P * 8, "ms_per_step": e2e_step * 1e3, "pairs_per_s": P * ws / e2e_step}
+    # parity spot check of the e2e copy (canonical pairs)
+    got = out_host.numpy().view(np.uint32)
+    assert (got[:, 0] < got[:, 1]).all()
+
+    # roofline of the dominant kernel
+    peak, peak_kind = peaks()
+    algo = algorithmic_bytes(stats, n)
+    share = {k: phase.get(k, 0.0) for k in algo}
+    top = max(share, key=lambda k: share[k])
+    ms = phase[top]
+    achieved = algo[top] / (ms * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tf):
+        try:
+            with open(tf) as f:
+                traffic = json.load(f).get(args.workload, {}).get(top)
+        except Exception:
+            traffic = None
+    kern = {k: {"ms": phase[k], "algorithmic_bytes": algo[k],
+                "achieved_gbs": algo[k] / (phase[k] * 1e-3) / 1e9 if phase[k] > 0 else None,
+                "frac_of_" + peak_kind: (algo[k] / (phase[k] * 1e-3) / 1e9) / peak if phase[k] > 0 else None}
+            for k in algo}
+    kern["pairs"]["pair_tests_per_s"] = stats["pair_tests"] / (phase["pairs"] * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": desc, "boxes": n, "pairs": P, "range": rng, "cell_shift": stats["cell_shift"],
+                   "entries": stats["entries"], "cells": stats["cells"], "pair_tests": stats["pair_tests"],
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "flushed between steps (256 MiB write)"},
+        "pairs_per_s": P * args.steps * ws / t_step,
+        "e2e": e2e,
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": algo[top]},
+        "kernels": kern,
+        "gpu_launches": kernels,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(boxes, rng, args.cpu_budget, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="clustered4m")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, local, ws = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+    else:
+        run_gb300(args, rank, local, ws)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,144 @@
+/*
+ * pbig2.h — C ABI of the GB300 pairwise box-intersection engine.
+ *
+ * Plain pointers and sizes only; no C++ or torch types. Every entry point
+ * returns a pbig2_status; pbig2_last_error() gives a message for the last
+ * failure on the calling thread.
+ *
+ * Boxes use PBIG's RectInfo layout (rect.h): per box 2*dims+1 unsigned ints
+ * {xmin,xmax,ymin,ymax[,zmin,zmax],rid}, rid equal to the box's index in its
+ * scene, every coordinate < range, min <= max. Two boxes overlap when their
+ * closed intervals intersect on every axis (touching faces count); a box
+ * never pairs with itself. Each overlapping pair is reported once.
+ *
+ * Reference interfaces replaced (paths in the awatch/pbig project):
+ *   pbig2_self_intersect    <- void pbig_check(RectInfo*, report*)
+ *                              src/pbig/pbig.h:10, src/pbig/pbig.cu:1962
+ *   pbig2_create/destroy    <- pbig_init / pbig_finalize
+ *                              src/pbig/pbig.h:9,11, src/pbig/pbig.cu:2139,141
+ *   pairs in device memory  <- the per-batch output stream + decode()
+ *                              src/pbig/pbig.cu:1694-1960, src/pbig/decode.cc:26
+ */
+#ifndef PBIG2_H_
+#define PBIG2_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define PBIG2_API __attribute__((visibility("default")))
+#else
+#define PBIG2_API
+#endif
+
+typedef enum {
+    PBIG2_OK = 0,
+    PBIG2_EINVAL = 1,    /* bad argument (null pointer, dims, sizes) */
+    PBIG2_ENOMEM = 2,    /* device or pinned allocation failed */
+    PBIG2_ECUDA = 3,     /* CUDA runtime error */
+    PBIG2_EINPUT = 4,    /* some boxes violate the input contract; they were
+                            skipped and the pairs of the others reported */
+    PBIG2_ETIMEOUT = 5,  /* a bounded device wait gave up */
+    PBIG2_ECAPACITY = 6, /* caller buffer too small; *count holds the need */
+    PBIG2_EBUSY = 7      /* serving queue full / admission refused */
+} pbig2_status;
+
+/* memory location flags for input/output buffers */
+#define PBIG2_HOST 0
+#define PBIG2_DEVICE 1
+
+typedef struct pbig2_ctx pbig2_ctx;
+
+/* Statistics of the last query on a context (all counts exact). */
+typedef struct {
+    uint64_t boxes;        /* boxes in the query */
+    uint64_t bad_boxes;    /* boxes rejected by the input contract */
+    uint64_t cells;        /* grid cells (sum over scenes) */
+    uint64_t entries;      /* cell entries E (box-in-cell records) */
+    uint64_t pair_tests;   /* sum over cells of n(n-1)/2 */
+    uint64_t pairs;        /* overlapping pairs reported */
+    uint32_t cell_shift;   /* log2(cell size) of the (first) scene */
+    uint32_t scenes;
+    uint32_t kernels;      /* kernel launches of the query */
+    uint32_t reserved;
+    double device_ms;      /* device time of the query (CUDA events) */
+    /* device time per phase of the last pipeline pass (CUDA events on the
+     * query's stream): count, scan, expand, scatter, pair test, grouping */
+    double phase_ms[6];
+} pbig2_stats;
+
+/* Context: one device, owns its buffers and streams. Not thread-safe; use
+ * one context per host thread. */
+PBIG2_API int pbig2_create(int device, pbig2_ctx** out);
+PBIG2_API int pbig2_destroy(pbig2_ctx* ctx);
+PBIG2_API const char* pbig2_last_error(void);
+PBIG2_API int pbig2_version(void);
+
+/* Self-intersection of one scene. `boxes` holds n RectInfo records in host
+ * (PBIG2_HOST) or device (PBIG2_DEVICE) memory. cell_shift selects the cell
+ * size 2^cell_shift; pass PBIG2_AUTO for the autotuner. `stream` is a
+ * cudaStream_t (NULL = the context's stream). The pairs stay resident on the
+ * device (pbig2_result_pairs) until the next query on the context; the call
+ * returns once the pair count is known and writes it to *npairs. */
+#define PBIG2_AUTO 0xffffffffu
+PBIG2_API int pbig2_self_intersect(pbig2_ctx* ctx, const uint32_t* boxes, uint64_t n, uint32_t dims,
+                                   uint32_t range, uint32_t cell_shift, int boxes_loc, void* stream,
+                                   uint64_t* npairs);
+
+/* Red/blue intersection: only pairs with one red and one blue box are
+ * reported, as (red index, blue index). */
+PBIG2_API int pbig2_bipartite_intersect(pbig2_ctx* ctx, const uint32_t* red, uint64_t n_red,
+                                        const uint32_t* blue, uint64_t n_blue, uint32_t dims,
+                                        uint32_t range, uint32_t cell_shift, int boxes_loc,
+                                        void* stream, uint64_t* npairs);
+
+/* Batched self-intersection of independent scenes in one launch sequence.
+ * `boxes` is the concatenation of all scenes (each scene's rid counts from
+ * 0); scene_offsets has n_scenes+1 entries (host memory). Pairs are grouped
+ * by scene: scene s owns result pairs [pair_offsets[s], pair_offsets[s+1])
+ * with scene-local indices (pbig2_result_scene_offsets). cell_shifts may be
+ * NULL (autotune every scene) or hold one shift per scene. */
+PBIG2_API int pbig2_batch_intersect(pbig2_ctx* ctx, const uint32_t* boxes,
+                                    const uint64_t* scene_offsets, uint32_t n_scenes, uint32_t dims,
+                                    uint32_t range, const uint32_t* cell_shifts, int boxes_loc,
+                                    void* stream, uint64_t* npairs);
+
+/* Result of the last query: device pointer to npairs uint32 pairs
+ * (a<b for self queries; (red,blue) for bipartite), valid until the next
+ * query on the context. */
+PBIG2_API int pbig2_result_pairs(pbig2_ctx* ctx, const uint32_t** dev_pairs, uint64_t* npairs);
+
+/* Copy pairs [first, first+count) of the last result into dst (host or
+ * device memory), in the result's order. */
+PBIG2_API int pbig2_copy_pairs(pbig2_ctx* ctx, uint32_t* dst, uint64_t first, uint64_t count,
+                               int dst_loc, void* stream);
+
+/* Per-scene pair offsets of the last batched query (n_scenes+1 values,
+ * host memory). */
+PBIG2_API int pbig2_result_scene_offsets(pbig2_ctx* ctx, uint64_t* offsets, uint32_t n_scenes);
+
+/* Asynchronous variant of pbig2_copy_pairs: enqueues the copy on `stream`
+ * and returns; pbig2_sync waits for it. */
+PBIG2_API int pbig2_copy_pairs_async(pbig2_ctx* ctx, uint32_t* dst, uint64_t first, uint64_t count,
+                                     int dst_loc, void* stream);
+PBIG2_API int pbig2_sync(pbig2_ctx* ctx, void* stream);
+
+/* Page-locked host memory for fast host<->device copies. */
+PBIG2_API int pbig2_host_alloc(size_t bytes, void** ptr);
+PBIG2_API int pbig2_host_free(void* ptr);
+
+PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
+
+/* Cell-size autotuner: the shift the engine would pick for these boxes
+ * (host memory), from a sample of at most `sample` boxes. */
+PBIG2_API int pbig2_tune_shift(const uint32_t* boxes, uint64_t n, uint32_t dims, uint32_t range,
+                               uint64_t sample, uint32_t* shift);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PBIG2_H_ */

@@ -1,0 +1,754 @@
+// Host orchestration of the pair-detection pipeline and the C ABI (pbig2.h).
+//
+// One query = one pass of count -> scan -> expand -> scatter -> pairs on the
+// context's stream, after the cell size has been chosen by the autotuner.
+// The reference runs the same phases with host round trips in between
+// (plan_phase / map_phase / sched_phase / match_phase, src/pbig/pbig.cu:1361,
+// 1429, 1592, 1694); here every phase stays on the device and the host reads
+// back one small counter block per query.
+#include "engine.h"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <unordered_map>
+
+namespace pbig {
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CK(expr)                                                                                   \
+    do {                                                                                           \
+        cudaError_t _e = (expr);                                                                   \
+        if (_e != cudaSuccess)                                                                     \
+            return fail(_e == cudaErrorMemoryAllocation ? PBIG2_ENOMEM : PBIG2_ECUDA, "%s: %s (%s:%d)", \
+                        #expr, cudaGetErrorString(_e), __FILE__, __LINE__);                        \
+    } while (0)
+
+cudaError_t DevBuf::ensure(size_t need, bool zero, cudaStream_t st) {
+    if (need == 0) need = 256;
+    if (need <= bytes) return cudaSuccess;
+    release();
+    size_t b = need + need / 8;
+    b = (b + 255) & ~size_t(255);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        return e;
+    }
+    bytes = b;
+    if (zero) return cudaMemsetAsync(p, 0, b, st);
+    return cudaSuccess;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+cudaError_t HostPinned::ensure(size_t need) {
+    if (need <= bytes) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMallocHost(&p, need);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        return e;
+    }
+    bytes = need;
+    return cudaSuccess;
+}
+
+void HostPinned::release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+uint32_t nrc_for(uint32_t range, uint32_t shift) {
+    return (uint32_t)(((uint64_t)range + (1ull << shift) - 1) >> shift);
+}
+
+// --------------------------------------------------------------------------
+// autotuner: cost(s) = kCell*C(s) + kEntry*E(s) + kTest*T(s) in seconds
+// (C cells, E box-in-cell entries, T pair tests), estimated from a sample.
+// T is counted exactly on the sample (cell occupancy by hashing) and scaled
+// by (n/m)^2, since a pair of boxes survives sampling with probability
+// (m/n)^2.
+// --------------------------------------------------------------------------
+static const double kCell = 1.2e-12, kEntry = 4.0e-12, kTest = 0.45e-12;
+
+// pair tests of the sample at one cell size: occupancy of the sample's cells
+// counted in an open-addressing hash table (key = cell id + 1)
+static double tests_in_sample(const uint32_t* boxes, const std::vector<uint64_t>& idx, int dims, uint32_t shift,
+                              uint32_t nrc, uint64_t nkeys, std::vector<uint64_t>& keys, std::vector<uint32_t>& cnt) {
+    const int W = 2 * dims + 1;
+    uint64_t cap = 64;
+    while (cap < 2 * nkeys) cap <<= 1;
+    keys.assign(cap, 0);
+    cnt.assign(cap, 0);
+    const uint64_t mask = cap - 1;
+    double t = 0;
+    for (uint64_t i : idx) {
+        const uint32_t* b = boxes + i * W;
+        uint32_t lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+        for (int d = 0; d < dims; d++) {
+            lo[d] = b[2 * d] >> shift;
+            hi[d] = b[2 * d + 1] >> shift;
+        }
+        for (uint32_t k = lo[2]; k <= hi[2]; k++)
+            for (uint32_t j = lo[1]; j <= hi[1]; j++)
+                for (uint32_t x = lo[0]; x <= hi[0]; x++) {
+                    const uint64_t key = ((uint64_t)k * nrc + j) * nrc + x + 1;
+                    uint64_t h = (key * 0x9e3779b97f4a7c15ULL) >> 20;
+                    for (;; h++) {
+                        uint64_t& slot = keys[h & mask];
+                        if (slot == key) break;
+                        if (slot == 0) { slot = key; break; }
+                    }
+                    t += cnt[h & mask]++;  // a new member pairs with every earlier one
+                }
+    }
+    return t;
+}
+
+static bool box_ok(const uint32_t* b, int dims, uint32_t range) {
+    for (int d = 0; d < dims; d++)
+        if (b[2 * d] > b[2 * d + 1] || b[2 * d + 1] >= range) return false;
+    return true;
+}
+
+// n is the number of boxes the sample idx stands for
+static TuneResult tune_impl(const uint32_t* boxes, const std::vector<uint64_t>& idx, uint64_t n, int dims,
+                            uint32_t range, bool exact_tests) {
+    const int W = 2 * dims + 1;
+    TuneResult best{0, 0, 0, 0};
+    if (idx.empty()) {
+        best.shift = 31;
+        while (best.shift > 0 && nrc_for(range, best.shift - 1) <= 1) best.shift--;
+        return best;
+    }
+    double mean_ext = 0;
+    uint64_t good = 0;
+    for (uint64_t i : idx) {
+        const uint32_t* b = boxes + i * W;
+        if (!box_ok(b, dims, range)) continue;
+        for (int d = 0; d < dims; d++) mean_ext += (double)(b[2 * d + 1] - b[2 * d]) + 1.0;
+        good++;
+    }
+    if (good == 0) good = 1;
+    mean_ext /= (double)(good * dims);
+    int s0 = (int)std::floor(std::log2(std::max(1.0, mean_ext)));
+    const double scale = (double)n / (double)idx.size();
+    std::vector<uint64_t> keys;
+    std::vector<uint32_t> cnts;
+    double best_cost = 1e300;
+    for (int s = std::max(0, s0 - 2); s <= std::min(31, s0 + 3); s++) {
+        const uint32_t nrc = nrc_for(range, (uint32_t)s);
+        const double C = std::pow((double)nrc, dims);
+        if (C > 4.0e9) continue;
+        double E = 0;
+        for (uint64_t i : idx) {
+            const uint32_t* b = boxes + i * W;
+            if (!box_ok(b, dims, range)) continue;
+            double c = 1;
+            for (int d = 0; d < dims; d++) c *= (double)((b[2 * d + 1] >> s) - (b[2 * d] >> s) + 1);
+            E += c;
+        }
+        if (E / (double)idx.size() > 64.0) continue;  // replication too high to be a candidate
+        const double Es = E;
+        E *= scale;
+        double T;
+        if (exact_tests) {
+            T = tests_in_sample(boxes, idx, dims, (uint32_t)s, nrc, (uint64_t)Es, keys, cnts) * scale * scale;
+        } else {
+            T = E * E / (2.0 * C);
+        }
+        const double cost = kCell * C + kEntry * E + kTest * T;
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = TuneResult{(uint32_t)s, E, T, C};
+        }
+    }
+    if (best_cost == 1e300) {  // fall back to the coarsest grid that is not a single cell
+        uint32_t s = 31;
+        while (s > 0 && nrc_for(range, s - 1) <= 1) s--;
+        best.shift = s;
+        best.est_cells = std::pow((double)nrc_for(range, s), dims);
+        best.est_entries = (double)n;
+        best.est_tests = (double)n * n / 2;
+    }
+    return best;
+}
+
+// boxes: n_avail records standing for n_true boxes (a sample when smaller)
+TuneResult tune_shift_sample(const uint32_t* boxes, uint64_t n_avail, uint64_t n_true, int dims, uint32_t range,
+                             uint64_t max_sample) {
+    std::vector<uint64_t> idx;
+    const uint64_t m = std::min<uint64_t>(n_avail, std::max<uint64_t>(1, max_sample));
+    idx.reserve(m);
+    for (uint64_t i = 0; i < m; i++) idx.push_back((uint64_t)((unsigned __int128)i * n_avail / m));
+    return tune_impl(boxes, idx, n_true, dims, range, true);
+}
+
+TuneResult tune_shift_analytic(const uint32_t* sample, uint64_t nsample, uint64_t n, int dims, uint32_t range) {
+    std::vector<uint64_t> idx(nsample);
+    for (uint64_t i = 0; i < nsample; i++) idx[i] = i;
+    return tune_impl(sample, idx, n, dims, range, false);
+}
+
+// --------------------------------------------------------------------------
+// pipeline
+// --------------------------------------------------------------------------
+struct GridScene {
+    uint64_t box_off, n;
+    uint32_t shift;
+    int grid_of;  // index of the scene whose grid this one shares (self for its own)
+};
+
+static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, int dims, uint32_t range,
+                        const std::vector<GridScene>& scenes, uint32_t split, double est_entries,
+                        cudaStream_t st, bool group) {
+    const uint32_t nsc = (uint32_t)scenes.size();
+    if (nboxes > (uint64_t)kIdMask + 1)
+        return fail(PBIG2_EINVAL, "a query holds at most 2^29 boxes (got %llu)", (unsigned long long)nboxes);
+    // scene table
+    std::vector<Scene> tab(nsc);
+    std::vector<uint32_t> box_off(nsc + 1);
+    uint64_t ncells = 0;
+    for (uint32_t i = 0; i < nsc; i++) {
+        const GridScene& g = scenes[i];
+        Scene& s = tab[i];
+        s.box_off = (uint32_t)g.box_off;
+        s.n = (uint32_t)g.n;
+        s.shift = g.shift;
+        s.nrc = nrc_for(range, g.shift);
+        s.range = range;
+        s.pad = 0;
+        if (g.grid_of == (int)i) {
+            s.cell_off = ncells;
+            uint64_t cc = s.nrc;
+            for (int d = 1; d < dims; d++) cc *= s.nrc;
+            ncells += cc;
+        } else {
+            s.cell_off = tab[g.grid_of].cell_off;
+        }
+        box_off[i] = (uint32_t)g.box_off;
+    }
+    box_off[nsc] = (uint32_t)nboxes;
+    if (ncells >= (1ull << 32) - 1)
+        return fail(PBIG2_EINVAL, "grid too fine: %llu cells (limit 2^32)", (unsigned long long)ncells);
+
+    const size_t tab_bytes = nsc * sizeof(Scene), off_bytes = (nsc + 1) * sizeof(uint32_t);
+    CK(c->h_stage.ensure(tab_bytes + off_bytes + 64));
+    CK(cudaStreamSynchronize(st));  // staging buffer reuse
+    memcpy(c->h_stage.p, tab.data(), tab_bytes);
+    memcpy((char*)c->h_stage.p + tab_bytes, box_off.data(), off_bytes);
+    CK(c->d_scenes.ensure(tab_bytes, false, st));
+    CK(c->d_scene_off.ensure(off_bytes, false, st));
+    CK(cudaMemcpyAsync(c->d_scenes.p, c->h_stage.p, tab_bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->d_scene_off.p, (char*)c->h_stage.p + tab_bytes, off_bytes, cudaMemcpyHostToDevice, st));
+
+    // capacities
+    const bool counts_new = c->d_counts.bytes < ncells * 4;
+    CK(c->d_counts.ensure(ncells * 4, true, st));
+    if (c->counts_dirty && !counts_new) CK(cudaMemsetAsync(c->d_counts.p, 0, c->d_counts.bytes, st));
+    c->counts_dirty = false;
+    CK(c->d_starts.ensure((ncells + 1) * 4 + 16, false, st));
+    const uint64_t tiles = scan_tiles(ncells);
+    CK(c->d_state.ensure(tiles * 8, false, st));
+    CK(c->d_ctr.ensure(sizeof(Ctr), false, st));
+    CK(c->h_ctr.ensure(sizeof(Ctr)));
+
+    uint64_t entry_cap = (uint64_t)(est_entries * 1.25) + 4096;
+    entry_cap = std::max<uint64_t>(entry_cap, c->d_entries.bytes / 4);
+    uint64_t out_cap = std::max<uint64_t>({c->out_hint, nboxes * 4, 1u << 16});
+    out_cap = std::max<uint64_t>(out_cap, c->d_out.bytes / 8);
+    uint64_t task_cap = std::max<uint64_t>(c->d_tasks.bytes / 16, 4096);
+
+    Params p{};
+    p.boxes = d_boxes;
+    p.nboxes = nboxes;
+    p.scenes = c->d_scenes.as<Scene>();
+    p.scene_box_off = c->d_scene_off.as<uint32_t>();
+    p.nscenes = nsc;
+    p.split = split;
+    p.ncells = ncells;
+    p.tile_state = c->d_state.as<unsigned long long>();
+    p.ctr = c->d_ctr.as<Ctr>();
+    const int grid = c->sm_count * pair_blocks_per_sm();
+    Ctr h{};
+    int launches = 0;
+    bool need_full = true;
+    c->counts_dirty = true;  // until a pass completes, counts may be non-zero
+    for (int attempt = 0; attempt < 6; attempt++) {
+        CK(c->d_entries.ensure(entry_cap * 4, false, st));
+        // list regions: a cell of class c holds at least lo_c boxes, so with
+        // E <= entry capacity no list can overflow
+        const uint64_t ecap = c->d_entries.bytes / 4;
+        const uint64_t lo[kNumLists] = {2, 5, 9, 17, 33, kBigMax + 1};
+        uint64_t loff = 0;
+        for (int k = 0; k < kNumLists; k++) {
+            p.list_off[k] = loff;
+            p.list_cap[k] = ecap / lo[k] + 1;
+            loff += p.list_cap[k];
+        }
+        CK(c->d_lists.ensure(loff * 4, false, st));
+        CK(c->d_tasks.ensure(task_cap * 16, false, st));
+        CK(c->d_out.ensure(out_cap * 8, false, st));
+        p.counts = c->d_counts.as<uint32_t>();
+        p.starts = c->d_starts.as<uint32_t>();
+        p.entries = c->d_entries.as<uint32_t>();
+        p.entry_cap = c->d_entries.bytes / 4;
+        p.lists = c->d_lists.as<uint32_t>();
+        p.tasks = c->d_tasks.as<uint4>();
+        p.task_cap = c->d_tasks.bytes / 16;
+        p.out = c->d_out.as<uint2>();
+        p.out_cap = c->d_out.bytes / 8;
+        if (attempt == 0) CK(cudaEventRecord(c->ev0, st));
+        if (need_full) {
+            CK(cudaMemsetAsync(p.ctr, 0, sizeof(Ctr), st));
+            CK(cudaMemsetAsync(p.tile_state, 0, tiles * 8, st));
+            CK(cudaEventRecord(c->evp[0], st));
+            CK(launch_count(p, dims, st));
+            CK(cudaEventRecord(c->evp[1], st));
+            CK(launch_scan(p, st));
+            CK(cudaEventRecord(c->evp[2], st));
+            CK(launch_expand(p, st));
+            CK(cudaEventRecord(c->evp[3], st));
+            CK(launch_scatter(p, dims, st));
+            CK(cudaEventRecord(c->evp[4], st));
+            launches += 4;
+        } else {
+            CK(cudaEventRecord(c->evp[4], st));
+            // keep the grid and lists; clear the pair count and error word
+            CK(cudaMemsetAsync(&p.ctr->pairs, 0, sizeof(unsigned long long), st));
+            CK(cudaMemsetAsync(&p.ctr->err, 0, sizeof(unsigned int), st));
+        }
+        CK(launch_pairs(p, dims, grid, st));
+        launches += 1;
+        CK(cudaEventRecord(c->evp[5], st));
+        CK(cudaEventRecord(c->ev1, st));
+        CK(cudaMemcpyAsync(c->h_ctr.p, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, st));
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            c->counts_dirty = true;
+            return fail(PBIG2_ECUDA, "pipeline failed: %s", cudaGetErrorString(e));
+        }
+        memcpy(&h, c->h_ctr.p, sizeof(Ctr));
+        c->counts_dirty = false;  // the scatter returned every count to zero
+        if (h.err & kErrWait) {
+            c->counts_dirty = true;
+            return fail(PBIG2_ETIMEOUT, "scan look-back wait gave up");
+        }
+        if (h.err & kErrIndex) {
+            c->counts_dirty = true;
+            return fail(PBIG2_ECUDA, "inconsistent cell lists (error bits 0x%x)", h.err);
+        }
+        if ((h.err & kErrEntryOvf) || h.entries > p.entry_cap) {
+            if (h.entries >= (1ull << 32))
+                return fail(PBIG2_ENOMEM, "%llu cell entries exceed the 2^32 limit of one query",
+                            (unsigned long long)h.entries);
+            entry_cap = h.entries + h.entries / 16 + 4096;
+            need_full = true;
+            continue;
+        }
+        if (h.err & kErrTaskOvf) {
+            task_cap = (uint64_t)h.need_tasks + 1024;
+            need_full = true;
+            continue;
+        }
+        if ((h.err & kErrOutOvf) || h.pairs > p.out_cap) {
+            out_cap = h.pairs + h.pairs / 8 + 1024;
+            need_full = false;
+            continue;
+        }
+        break;
+    }
+    if (h.err & (kErrEntryOvf | kErrTaskOvf | kErrOutOvf)) return fail(PBIG2_ENOMEM, "capacity retries exhausted");
+    c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    double phase[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 5; k++) {
+        float x = 0;
+        if (cudaEventElapsedTime(&x, c->evp[k], c->evp[k + 1]) == cudaSuccess) phase[k] = x;
+    }
+
+    c->npairs = h.pairs;
+    c->result = c->d_out.as<uint2>();
+    c->scene_pair_off.assign(1, 0);
+    if (group && nsc > 1) {
+        // histogram of pairs per scene on the host from the device copy is too
+        // slow for large outputs; count on the device instead.
+        CK(c->d_scene_pair.ensure((nsc + 1) * 8, false, st));
+        CK(c->d_scene_cursor.ensure((nsc + 1) * 8, false, st));
+        CK(c->d_out2.ensure(std::max<uint64_t>(h.pairs, 1) * 8, false, st));
+        CK(cudaMemsetAsync(c->d_scene_cursor.p, 0, (nsc + 1) * 8, st));
+        Params q = p;
+        q.out_cap = h.pairs;
+        CK(launch_scene_hist(q, c->d_scene_cursor.as<unsigned long long>(), st));
+        std::vector<unsigned long long> hist(nsc + 1);
+        CK(c->h_stage.ensure((nsc + 1) * 8));
+        CK(cudaMemcpyAsync(c->h_stage.p, c->d_scene_cursor.p, (nsc + 1) * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        memcpy(hist.data(), c->h_stage.p, (nsc + 1) * 8);
+        c->scene_pair_off.assign(nsc + 1, 0);
+        for (uint32_t i = 0; i < nsc; i++) c->scene_pair_off[i + 1] = c->scene_pair_off[i] + hist[i];
+        memcpy(c->h_stage.p, c->scene_pair_off.data(), (nsc + 1) * 8);
+        CK(cudaMemcpyAsync(c->d_scene_pair.p, c->h_stage.p, (nsc + 1) * 8, cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(c->d_scene_cursor.p, 0, (nsc + 1) * 8, st));
+        CK(launch_group_by_scene(q, c->d_scene_pair.as<unsigned long long>(),
+                                 c->d_scene_cursor.as<unsigned long long>(), c->d_out2.as<uint2>(), st));
+        CK(cudaEventRecord(c->ev1, st));
+        CK(cudaStreamSynchronize(st));
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        float x = 0;
+        if (cudaEventElapsedTime(&x, c->evp[5], c->ev1) == cudaSuccess) phase[5] = x;
+        c->result = c->d_out2.as<uint2>();
+        launches += 2;
+    } else {
+        c->scene_pair_off.push_back(h.pairs);
+    }
+    pbig2_stats& s = c->stats;
+    s.boxes = nboxes;
+    s.bad_boxes = h.bad;
+    s.cells = ncells;
+    s.entries = h.entries;
+    s.pair_tests = h.tests;
+    s.pairs = h.pairs;
+    s.cell_shift = scenes.empty() ? 0 : scenes[0].shift;
+    s.scenes = nsc;
+    s.kernels = (uint32_t)launches;
+    s.device_ms = ms;
+    for (int k = 0; k < 6; k++) s.phase_ms[k] = phase[k];
+    if (h.bad) return fail(PBIG2_EINPUT, "%u boxes violate the input contract (error bits 0x%x) and were skipped",
+                           h.bad, h.err);
+    return PBIG2_OK;
+}
+
+static cudaStream_t pick_stream(pbig2_ctx* c, void* stream) {
+    return stream ? (cudaStream_t)stream : c->own_stream;
+}
+
+// strided sample of device-resident boxes (host copy) for the autotuner
+static int sample_device_boxes(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t n, int dims, uint64_t m,
+                               cudaStream_t st, std::vector<uint32_t>& out) {
+    const int W = 2 * dims + 1;
+    m = std::min<uint64_t>(m, n);
+    out.resize(m * W);
+    if (m == 0) return PBIG2_OK;
+    CK(c->h_stage.ensure(m * W * 4));
+    const uint64_t stride = n / m;
+    CK(cudaMemcpy2DAsync(c->h_stage.p, W * 4, d_boxes, stride * W * 4, W * 4, m, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    memcpy(out.data(), c->h_stage.p, m * W * 4);
+    return PBIG2_OK;
+}
+
+static int stage_boxes_in(pbig2_ctx* c, const uint32_t* boxes, uint64_t words, int loc, cudaStream_t st,
+                          const uint32_t** d_boxes) {
+    if (loc == PBIG2_DEVICE) {
+        *d_boxes = boxes;
+        return PBIG2_OK;
+    }
+    CK(c->d_boxes.ensure(words * 4, false, st));
+    CK(cudaMemcpyAsync(c->d_boxes.p, boxes, words * 4, cudaMemcpyHostToDevice, st));
+    *d_boxes = c->d_boxes.as<uint32_t>();
+    return PBIG2_OK;
+}
+
+}  // namespace pbig
+
+using namespace pbig;
+
+extern "C" {
+
+PBIG2_API const char* pbig2_last_error(void) { return g_last_error.c_str(); }
+
+PBIG2_API int pbig2_version(void) { return 1; }
+
+PBIG2_API int pbig2_create(int device, pbig2_ctx** out) {
+    if (!out) return fail(PBIG2_EINVAL, "out is null");
+    *out = nullptr;
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(PBIG2_EINVAL, "device %d out of range (%d devices)", device, ndev);
+    CK(cudaSetDevice(device));
+    pbig2_ctx* c = new pbig2_ctx();
+    c->device = device;
+    cudaError_t e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    for (int k = 0; k < 7 && e == cudaSuccess; k++) e = cudaEventCreate(&c->evp[k]);
+    if (e == cudaSuccess) e = kernels_init();
+    if (e != cudaSuccess) {
+        pbig2_destroy(c);
+        return fail(PBIG2_ECUDA, "context setup: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
+    if (!c) return PBIG2_OK;
+    cudaSetDevice(c->device);
+    if (c->own_stream) cudaStreamSynchronize(c->own_stream);
+    for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_starts, &c->d_entries, &c->d_lists, &c->d_tasks, &c->d_state,
+                      &c->d_out, &c->d_out2, &c->d_ctr, &c->d_scenes, &c->d_scene_off, &c->d_scene_pair,
+                      &c->d_scene_cursor})
+        b->release();
+    c->h_ctr.release();
+    c->h_stage.release();
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (cudaEvent_t ev : c->evp)
+        if (ev) cudaEventDestroy(ev);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_tune_shift(const uint32_t* boxes, uint64_t n, uint32_t dims, uint32_t range, uint64_t sample,
+                               uint32_t* shift) {
+    if (!boxes || !shift || (dims != 2 && dims != 3) || range == 0) return fail(PBIG2_EINVAL, "bad arguments");
+    *shift = tune_shift_sample(boxes, n, n, (int)dims, range, sample ? sample : 4096).shift;
+    return PBIG2_OK;
+}
+
+// autotuner with a per-context memo: a query whose size, dims, range and
+// mean box extent (over 256 strided boxes) match an earlier one within 5%
+// reuses that choice
+static TuneResult memo_tune(pbig2_ctx* c, const uint32_t* boxes, uint64_t n_avail, uint64_t n, int dims,
+                            uint32_t range, uint64_t sample) {
+    const int W = 2 * dims + 1;
+    const uint64_t m = std::min<uint64_t>(n_avail, 256);
+    double ext = 0;
+    for (uint64_t i = 0; i < m; i++) {
+        const uint32_t* b = boxes + (uint64_t)((unsigned __int128)i * n_avail / m) * W;
+        for (int d = 0; d < dims; d++) ext += (double)b[2 * d + 1] - (double)b[2 * d];
+    }
+    ext = m ? ext / (double)(m * dims) : 0;
+    for (const auto& e : c->memo)
+        if (e.dims == dims && e.range == range && std::fabs((double)e.n - (double)n) <= 0.05 * (double)n &&
+            std::fabs(e.ext - ext) <= 0.05 * std::max(1.0, e.ext))
+            return TuneResult{e.shift, e.est_e * (double)n / std::max(1.0, (double)e.n), 0, 0};
+    TuneResult tr = tune_shift_sample(boxes, n_avail, n, dims, range, sample);
+    if (c->memo.size() >= 64) c->memo.erase(c->memo.begin());
+    c->memo.push_back({n, dims, range, ext, tr.shift, tr.est_entries});
+    return tr;
+}
+
+static int self_or_bip(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const uint32_t* blue, uint64_t n_blue,
+                       uint32_t dims, uint32_t range, uint32_t cell_shift, int loc, void* stream, uint64_t* npairs) {
+    if (!c || !npairs || (dims != 2 && dims != 3) || range == 0) return fail(PBIG2_EINVAL, "bad arguments");
+    if ((n_red && !red) || (n_blue && !blue)) return fail(PBIG2_EINVAL, "null box pointer");
+    if (cell_shift != PBIG2_AUTO && cell_shift > 31) return fail(PBIG2_EINVAL, "cell_shift %u > 31", cell_shift);
+    *npairs = 0;
+    CK(cudaSetDevice(c->device));
+    cudaStream_t st = pick_stream(c, stream);
+    const int W = 2 * (int)dims + 1;
+    const bool bip = blue != nullptr;
+    const uint64_t n = n_red + n_blue;
+    const uint32_t* d_boxes = nullptr;
+    if (!bip) {
+        int rc = stage_boxes_in(c, red, n_red * W, loc, st, &d_boxes);
+        if (rc) return rc;
+    } else {
+        CK(c->d_boxes.ensure(n * W * 4 + 16, false, st));
+        const cudaMemcpyKind k = loc == PBIG2_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        if (n_red) CK(cudaMemcpyAsync(c->d_boxes.p, red, n_red * W * 4, k, st));
+        if (n_blue) CK(cudaMemcpyAsync(c->d_boxes.as<uint32_t>() + n_red * W, blue, n_blue * W * 4, k, st));
+        d_boxes = c->d_boxes.as<uint32_t>();
+    }
+    // choose the cell size (from a sample of the union for red/blue)
+    TuneResult tr{};
+    std::vector<uint32_t> smp;
+    const uint64_t kSample = 4096;
+    if (cell_shift != PBIG2_AUTO) {
+        tr.shift = cell_shift;
+    } else if (loc == PBIG2_HOST && !bip) {
+        tr = memo_tune(c, red, n, n, (int)dims, range, kSample);
+    } else {
+        if (loc == PBIG2_HOST) {
+            const uint64_t m = std::min<uint64_t>(n, kSample);
+            smp.resize(m * W);
+            for (uint64_t i = 0; i < m; i++) {
+                const uint64_t g = (uint64_t)((unsigned __int128)i * n / m);
+                const uint32_t* src = g < n_red ? red + g * W : blue + (g - n_red) * W;
+                memcpy(&smp[i * W], src, W * 4);
+            }
+        } else {
+            int rc = sample_device_boxes(c, d_boxes, n, (int)dims, kSample, st, smp);
+            if (rc) return rc;
+        }
+        tr = memo_tune(c, smp.data(), smp.size() / W, n, (int)dims, range, kSample);
+    }
+    std::vector<GridScene> sc;
+    if (!bip) {
+        sc.push_back({0, n, tr.shift, 0});
+    } else {
+        sc.push_back({0, n_red, tr.shift, 0});
+        sc.push_back({n_red, n_blue, tr.shift, 0});
+    }
+    int rc = run_pipeline(c, d_boxes, n, (int)dims, range, sc, bip ? (uint32_t)n_red : kNoSplit,
+                          std::max(tr.est_entries, (double)n), st, false);
+    *npairs = c->npairs;
+    return rc;
+}
+
+PBIG2_API int pbig2_self_intersect(pbig2_ctx* c, const uint32_t* boxes, uint64_t n, uint32_t dims, uint32_t range,
+                                   uint32_t cell_shift, int boxes_loc, void* stream, uint64_t* npairs) {
+    return self_or_bip(c, boxes, n, nullptr, 0, dims, range, cell_shift, boxes_loc, stream, npairs);
+}
+
+PBIG2_API int pbig2_bipartite_intersect(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const uint32_t* blue,
+                                        uint64_t n_blue, uint32_t dims, uint32_t range, uint32_t cell_shift,
+                                        int boxes_loc, void* stream, uint64_t* npairs) {
+    if (!blue && n_blue == 0) {
+        static const uint32_t dummy[8] = {0};
+        blue = dummy;
+    }
+    return self_or_bip(c, red, n_red, blue, n_blue, dims, range, cell_shift, boxes_loc, stream, npairs);
+}
+
+PBIG2_API int pbig2_batch_intersect(pbig2_ctx* c, const uint32_t* boxes, const uint64_t* scene_offsets,
+                                    uint32_t n_scenes, uint32_t dims, uint32_t range, const uint32_t* cell_shifts,
+                                    int boxes_loc, void* stream, uint64_t* npairs) {
+    if (!c || !npairs || !scene_offsets || (dims != 2 && dims != 3) || range == 0 || n_scenes == 0)
+        return fail(PBIG2_EINVAL, "bad arguments");
+    *npairs = 0;
+    CK(cudaSetDevice(c->device));
+    cudaStream_t st = pick_stream(c, stream);
+    const int W = 2 * (int)dims + 1;
+    const uint64_t n = scene_offsets[n_scenes];
+    for (uint32_t i = 0; i < n_scenes; i++)
+        if (scene_offsets[i + 1] < scene_offsets[i]) return fail(PBIG2_EINVAL, "scene offsets must not decrease");
+    if (n && !boxes) return fail(PBIG2_EINVAL, "null boxes");
+    const uint32_t* d_boxes = nullptr;
+    int rc = stage_boxes_in(c, boxes, n * W, boxes_loc, st, &d_boxes);
+    if (rc) return rc;
+    // per-scene cell size: analytic tuner on a small per-scene sample
+    std::vector<GridScene> sc(n_scenes);
+    double est_e = 0;
+    const uint64_t kPer = 64;
+    std::vector<uint32_t> smp;
+    if (!cell_shifts && boxes_loc == PBIG2_DEVICE) {
+        // one strided copy per scene would be thousands of calls; sample the
+        // whole batch once and attribute sample boxes to their scenes
+        rc = sample_device_boxes(c, d_boxes, n, (int)dims, std::min<uint64_t>(n, kPer * n_scenes), st, smp);
+        if (rc) return rc;
+    }
+    const uint64_t msmp = smp.size() / W;
+    uint64_t sp = 0;
+    for (uint32_t i = 0; i < n_scenes; i++) {
+        const uint64_t a = scene_offsets[i], b = scene_offsets[i + 1], ns = b - a;
+        uint32_t shift;
+        double e = (double)ns;
+        if (cell_shifts) {
+            shift = cell_shifts[i];
+            if (shift > 31) return fail(PBIG2_EINVAL, "cell_shifts[%u] > 31", i);
+        } else if (boxes_loc == PBIG2_HOST) {
+            const uint64_t m = std::min<uint64_t>(ns, kPer);
+            std::vector<uint32_t> s(m * W);
+            for (uint64_t k = 0; k < m; k++)
+                memcpy(&s[k * W], boxes + (a + (uint64_t)((unsigned __int128)k * ns / m)) * W, W * 4);
+            TuneResult tr = tune_shift_analytic(s.data(), m, ns, (int)dims, range);
+            shift = tr.shift;
+            e = std::max(e, tr.est_entries);
+        } else {
+            // sample boxes g*stride that fall inside [a, b)
+            const uint64_t stride = msmp ? n / msmp : 1;
+            const uint64_t s0 = sp;
+            while (sp < msmp && sp * stride < b) sp++;
+            TuneResult tr = tune_shift_analytic(smp.data() + s0 * W, sp - s0, ns, (int)dims, range);
+            shift = tr.shift;
+            e = std::max(e, tr.est_entries);
+        }
+        sc[i] = GridScene{a, ns, shift, (int)i};
+        est_e += e;
+    }
+    rc = run_pipeline(c, d_boxes, n, (int)dims, range, sc, kNoSplit, est_e, st, true);
+    *npairs = c->npairs;
+    return rc;
+}
+
+PBIG2_API int pbig2_result_pairs(pbig2_ctx* c, const uint32_t** dev_pairs, uint64_t* npairs) {
+    if (!c || !dev_pairs || !npairs) return fail(PBIG2_EINVAL, "bad arguments");
+    *dev_pairs = reinterpret_cast<const uint32_t*>(c->result);
+    *npairs = c->npairs;
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_copy_pairs(pbig2_ctx* c, uint32_t* dst, uint64_t first, uint64_t count, int dst_loc,
+                               void* stream) {
+    if (!c || (count && !dst)) return fail(PBIG2_EINVAL, "bad arguments");
+    if (first > c->npairs || count > c->npairs - first) return fail(PBIG2_EINVAL, "range beyond the result");
+    if (count == 0) return PBIG2_OK;
+    CK(cudaSetDevice(c->device));
+    cudaStream_t st = pick_stream(c, stream);
+    const cudaMemcpyKind k = dst_loc == PBIG2_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    CK(cudaMemcpyAsync(dst, c->result + first, count * 8, k, st));
+    if (dst_loc != PBIG2_DEVICE) CK(cudaStreamSynchronize(st));
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_copy_pairs_async(pbig2_ctx* c, uint32_t* dst, uint64_t first, uint64_t count, int dst_loc,
+                                     void* stream) {
+    if (!c || (count && !dst)) return fail(PBIG2_EINVAL, "bad arguments");
+    if (first > c->npairs || count > c->npairs - first) return fail(PBIG2_EINVAL, "range beyond the result");
+    if (count == 0) return PBIG2_OK;
+    CK(cudaSetDevice(c->device));
+    const cudaMemcpyKind k = dst_loc == PBIG2_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    CK(cudaMemcpyAsync(dst, c->result + first, count * 8, k, pick_stream(c, stream)));
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_sync(pbig2_ctx* c, void* stream) {
+    if (!c) return fail(PBIG2_EINVAL, "bad arguments");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(pick_stream(c, stream)));
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return fail(PBIG2_EINVAL, "bad arguments");
+    *ptr = nullptr;
+    CK(cudaMallocHost(ptr, bytes ? bytes : 1));
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_host_free(void* ptr) {
+    if (ptr) CK(cudaFreeHost(ptr));
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_result_scene_offsets(pbig2_ctx* c, uint64_t* offsets, uint32_t n_scenes) {
+    if (!c || !offsets) return fail(PBIG2_EINVAL, "bad arguments");
+    if (c->scene_pair_off.size() != (size_t)n_scenes + 1)
+        return fail(PBIG2_EINVAL, "last result has %zu scenes", c->scene_pair_off.size() - 1);
+    memcpy(offsets, c->scene_pair_off.data(), (n_scenes + 1) * 8);
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_get_stats(pbig2_ctx* c, pbig2_stats* s) {
+    if (!c || !s) return fail(PBIG2_EINVAL, "bad arguments");
+    *s = c->stats;
+    return PBIG2_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+// Host-side engine: owns device buffers and runs the pipeline.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+#include "pbig2.h"
+
+namespace pbig {
+
+// grow-only device allocation
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need, bool zero, cudaStream_t st);
+    void release();
+    template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct HostPinned {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need);
+    void release();
+};
+
+struct SceneIn {
+    uint64_t box_off, n;
+    uint32_t shift;   // chosen cell shift
+};
+
+// cell-size autotuner (host): cost model over candidate shifts, fed from a
+// sample of boxes. `words` = 2*dims+1.
+struct TuneResult {
+    uint32_t shift;
+    double est_entries, est_tests, est_cells;
+};
+TuneResult tune_shift_sample(const uint32_t* boxes, uint64_t n_avail, uint64_t n_true, int dims, uint32_t range,
+                             uint64_t max_sample);
+TuneResult tune_shift_analytic(const uint32_t* sample, uint64_t nsample, uint64_t n, int dims, uint32_t range);
+uint32_t nrc_for(uint32_t range, uint32_t shift);
+
+}  // namespace pbig
+
+struct pbig2_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t evp[7] = {};
+    pbig::DevBuf d_boxes, d_counts, d_starts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
+        d_scenes, d_scene_off, d_scene_pair, d_scene_cursor;
+    pbig::HostPinned h_ctr, h_stage;
+    bool counts_dirty = false;
+    // last result
+    const uint2* result = nullptr;
+    uint64_t npairs = 0;
+    std::vector<uint64_t> scene_pair_off;
+    pbig2_stats stats{};
+    // capacity hints carried between queries
+    uint64_t out_hint = 0;
+    // autotuner memo: (n, dims, range, mean extent) -> shift
+    struct TuneMemo { uint64_t n; int dims; uint32_t range; double ext; uint32_t shift; double est_e; };
+    std::vector<TuneMemo> memo;
+};

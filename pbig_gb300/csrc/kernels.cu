@@ -1,0 +1,828 @@
+// Kernels of the GB300 pairwise box-intersection pipeline.
+//
+//   k_count    boxes -> per-cell counts                (src/pbig/pbig.cu:174-221)
+//   k_scan     counts -> cell starts + cell work lists (host thrust scan, pbig.cu:1497-1505,
+//              and the job list of sched_phase, pbig.cu:1586-1688)
+//   k_expand   tile tasks for cells too big for shared memory (sched_phase's 256-row jobs)
+//   k_scatter  boxes -> cell entry lists               (d_mapping, pbig.cu:321-427)
+//   k_pairs    per-cell all-pairs test with the reference-cell rule and compacted output
+//              (d_matching + prefix_scan, pbig.cu:429-543, 562-603, 641-932)
+//
+// Box records are the reference's RectInfo (rect.h): 2*D+1 unsigned words.
+// Cell ids follow the reference linearisation gid = (k*nrc + j)*nrc + i.
+// An entry stores the box index and three "starts here" bits: bit d is set
+// when the box's minimum along axis d lies in this cell. The reference-cell
+// rule of calcRightToWrite (pbig.cu:579-603) -- a pair is reported in the
+// cell holding the minimum corner of the two boxes' intersection -- is then
+// exactly (flags_a | flags_b) == 7: along each axis max(min_a, min_b) falls
+// in this cell iff one of the two minima does (both boxes cover the cell).
+#include "kernels.cuh"
+
+#include <cstdio>
+
+namespace pbig {
+
+#define FULL_MASK 0xffffffffu
+
+__host__ __device__ __forceinline__ unsigned long long mn64(unsigned long long a, unsigned long long b) {
+    return a < b ? a : b;
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(FULL_MASK, v, o);
+        if (lane_id() >= o) v += t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    return v;
+}
+
+__device__ __forceinline__ uint32_t find_scene(const Params& p, uint64_t gi) {
+    if (p.nscenes <= 1) return 0;
+    uint32_t lo = 0, hi = p.nscenes;  // last scene s with scene_box_off[s] <= gi
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (p.scene_box_off[mid] <= gi) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// count / scatter: one thread per box, boxes staged through shared memory with
+// 16-byte vector loads; the cells of the 32 boxes of a warp are enumerated
+// cooperatively (lane q handles cell q of the warp's concatenated cell list),
+// so a box spanning many cells does not stall its warp.
+// ---------------------------------------------------------------------------
+constexpr int kBoxThreads = 256;
+
+template <int D>
+__device__ __forceinline__ void stage_boxes(const Params& p, uint64_t b0, uint32_t nb, uint32_t* sbox) {
+    constexpr uint32_t W = 2 * D + 1;
+    const uint32_t* src = p.boxes + b0 * W;
+    const uint32_t nwords = nb * W;
+    if (((reinterpret_cast<uintptr_t>(src) & 15u) == 0) && (nwords & 3u) == 0) {
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(sbox);
+        for (uint32_t k = threadIdx.x; k < nwords / 4; k += blockDim.x) d4[k] = __ldg(s4 + k);
+    } else {
+        for (uint32_t k = threadIdx.x; k < nwords; k += blockDim.x) sbox[k] = __ldg(src + k);
+    }
+}
+
+template <int D, bool SCATTER>
+__device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t* sbox, uint64_t b0,
+                                                uint32_t nb) {
+    constexpr uint32_t W = 2 * D + 1;
+    const uint32_t t = threadIdx.x, lane = t & 31u;
+    const uint64_t gi = b0 + t;
+    uint32_t cnt = 0, sx = 1, sy = 1, nrc = 0;
+    uint64_t base = 0;
+    if (t < nb) {
+        const uint32_t* b = sbox + t * W;
+        const Scene sc = p.scenes[find_scene(p, gi)];
+        uint32_t err = 0;
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            if (b[2 * d] >= sc.range || b[2 * d + 1] >= sc.range) err |= kErrRange;
+            if (b[2 * d] > b[2 * d + 1]) err |= kErrInverted;
+        }
+        if (b[2 * D] != (uint32_t)(gi - sc.box_off)) err |= kErrRid;
+        if (gi > kIdMask) err |= kErrIndex;
+        if (!err) {
+            const uint32_t sh = sc.shift;
+            const uint32_t lo0 = b[0] >> sh, lo1 = b[2] >> sh, lo2 = D == 3 ? (b[4] >> sh) : 0u;
+            sx = (b[1] >> sh) - lo0 + 1;
+            sy = (b[3] >> sh) - lo1 + 1;
+            const uint32_t sz = D == 3 ? (b[5] >> sh) - lo2 + 1 : 1u;
+            const uint64_t c64 = (uint64_t)sx * sy * sz;
+            if (c64 >= (1ull << 26)) {
+                err |= kErrCellOvf;
+            } else {
+                cnt = (uint32_t)c64;
+                nrc = sc.nrc;
+                base = sc.cell_off + ((uint64_t)lo2 * nrc + lo1) * nrc + lo0;
+            }
+        }
+        if (err && !SCATTER) {
+            atomicOr(&p.ctr->err, err);
+            atomicAdd(&p.ctr->bad, 1u);
+        }
+    }
+    const uint32_t incl = warp_incl_scan(cnt);
+    const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+    const uint32_t excl = incl - cnt;
+    const uint64_t wbox0 = b0 + (t & ~31u);
+    for (uint32_t q0 = 0; q0 < total; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        uint32_t o = 0;  // owner lane: number of lanes whose inclusive count <= q
+#pragma unroll
+        for (uint32_t step = 16; step; step >>= 1) {
+            const uint32_t v = __shfl_sync(FULL_MASK, incl, o + step - 1);
+            if (v <= q) o += step;
+        }
+        const uint32_t o_excl = __shfl_sync(FULL_MASK, excl, o);
+        const uint32_t o_sx = __shfl_sync(FULL_MASK, sx, o);
+        const uint32_t o_sy = __shfl_sync(FULL_MASK, sy, o);
+        const uint32_t o_nrc = __shfl_sync(FULL_MASK, nrc, o);
+        const uint64_t o_base = __shfl_sync(FULL_MASK, base, o);
+        if (q < total) {
+            const uint32_t lq = q - o_excl;
+            const uint32_t i = lq % o_sx, rr = lq / o_sx;
+            const uint32_t j = rr % o_sy, k = rr / o_sy;
+            const uint64_t gid = o_base + ((uint64_t)k * o_nrc + j) * o_nrc + i;
+            if (SCATTER) {
+                const uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
+                const uint32_t slot = atomicSub(&p.counts[gid], 1u) - 1u;
+                const uint64_t pos = (uint64_t)p.starts[gid] + slot;
+                if (pos < p.entry_cap) p.entries[pos] = (f << kIdBits) | (uint32_t)(wbox0 + o);
+                else atomicOr(&p.ctr->err, kErrEntryOvf);
+            } else {
+                atomicAdd(&p.counts[gid], 1u);
+            }
+        }
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBoxThreads) k_count(Params p) {
+    __shared__ __align__(16) uint32_t sbox[kBoxThreads * (2 * D + 1)];
+    const uint64_t b0 = (uint64_t)blockIdx.x * kBoxThreads;
+    const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
+    stage_boxes<D>(p, b0, nb, sbox);
+    __syncthreads();
+    enumerate_cells<D, false>(p, sbox, b0, nb);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBoxThreads) k_scatter(Params p) {
+    __shared__ __align__(16) uint32_t sbox[kBoxThreads * (2 * D + 1)];
+    const uint64_t b0 = (uint64_t)blockIdx.x * kBoxThreads;
+    const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
+    stage_boxes<D>(p, b0, nb, sbox);
+    __syncthreads();
+    enumerate_cells<D, true>(p, sbox, b0, nb);
+}
+
+// ---------------------------------------------------------------------------
+// scan: single-pass exclusive scan with decoupled look-back. A tile is 4096
+// cells: each warp owns 512 consecutive cells as 4 rows of 128, a lane 4
+// consecutive cells per row (one 16-byte load). Tile order is taken from an
+// atomic ticket so every tile only waits on tiles already running. The same
+// pass classifies cells into the work lists of the pair kernel.
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanTile = 4096;
+constexpr unsigned long long kFlagAgg = 1ull << 62, kFlagPre = 2ull << 62;
+constexpr unsigned long long kValMask = (1ull << 62) - 1;
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+__device__ __forceinline__ int list_of(uint32_t n) {
+    if (n < 2) return -1;
+    if (n <= 4) return 0;
+    if (n <= 8) return 1;
+    if (n <= 16) return 2;
+    if (n <= 32) return 3;
+    if (n <= kBigMax) return kListBig;
+    return kListHuge;
+}
+
+__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* a) {
+    return *reinterpret_cast<const volatile unsigned long long*>(a);
+}
+__device__ __forceinline__ void st_volatile(unsigned long long* a, unsigned long long v) {
+    *reinterpret_cast<volatile unsigned long long*>(a) = v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(Params p) {
+    __shared__ uint32_t s_tile;
+    __shared__ unsigned long long s_warp_tot[8];
+    __shared__ unsigned long long s_prefix;
+    __shared__ uint32_t s_cls[kNumLists], s_cls_base[kNumLists];
+    __shared__ unsigned long long s_tests;
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    if (t == 0) {
+        s_tile = atomicAdd(&p.ctr->ticket, 1u);
+        s_tests = 0;
+    }
+    if (t < kNumLists) s_cls[t] = 0;
+    __syncthreads();
+    const uint64_t tile = s_tile;
+    const uint64_t c_warp = tile * kScanTile + (uint64_t)warp * 512;  // first cell of this warp
+    // load 4 rows x 4 cells per lane
+    uint32_t v[16];
+    const bool full = tile * kScanTile + kScanTile <= p.ncells;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const uint64_t c = c_warp + (uint64_t)r * 128 + lane * 4;
+        if (full) {
+            const uint4 q = __ldcs(reinterpret_cast<const uint4*>(p.counts + c));
+            v[4 * r] = q.x; v[4 * r + 1] = q.y; v[4 * r + 2] = q.z; v[4 * r + 3] = q.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) v[4 * r + k] = (c + k < p.ncells) ? p.counts[c + k] : 0u;
+        }
+    }
+    // per-row lane sums and warp scans (64-bit running totals)
+    unsigned long long row_excl[4];
+    unsigned long long wtot = 0;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const uint32_t s = v[4 * r] + v[4 * r + 1] + v[4 * r + 2] + v[4 * r + 3];
+        // lane sums fit 32 bits for < 2^30 boxes per cell
+        const uint32_t inc = warp_incl_scan(s);
+        row_excl[r] = wtot + (inc - s);
+        wtot += __shfl_sync(FULL_MASK, inc, 31);
+    }
+    if (lane == 0) s_warp_tot[warp] = wtot;
+    __syncthreads();
+    unsigned long long warp_excl = 0, agg = 0;
+#pragma unroll
+    for (int w = 0; w < 8; w++) {
+        const unsigned long long x = s_warp_tot[w];
+        if (w < (int)warp) warp_excl += x;
+        agg += x;
+    }
+    // decoupled look-back (warp 0)
+    if (warp == 0) {
+        unsigned long long excl = 0;
+        if (tile == 0) {
+            if (lane == 0) st_volatile(&p.tile_state[0], kFlagPre | agg);
+        } else {
+            if (lane == 0) st_volatile(&p.tile_state[tile], kFlagAgg | agg);
+            long long look = (long long)tile - 1;
+            uint32_t spins = 0;
+            for (;;) {
+                const long long idx = look - (long long)lane;
+                const unsigned long long s = idx >= 0 ? ld_volatile(&p.tile_state[idx]) : kFlagPre;
+                if (__any_sync(FULL_MASK, (s >> 62) == 0)) {
+                    if (++spins > kSpinLimit) {
+                        if (lane == 0) atomicOr(&p.ctr->err, kErrWait);
+                        break;
+                    }
+                    continue;
+                }
+                const uint32_t pm = __ballot_sync(FULL_MASK, (s >> 62) == 2);
+                if (pm) {
+                    const uint32_t first = __ffs(pm) - 1;
+                    excl += warp_sum_u64(lane <= first ? (s & kValMask) : 0ull);
+                    break;
+                }
+                excl += warp_sum_u64(s & kValMask);
+                look -= 32;
+            }
+            if (lane == 0) st_volatile(&p.tile_state[tile], kFlagPre | (excl + agg));
+        }
+        if (lane == 0) s_prefix = excl;
+    }
+    __syncthreads();
+    const unsigned long long base = s_prefix + warp_excl;
+    // write starts and classify cells
+    uint32_t my_cls[kNumLists] = {0, 0, 0, 0, 0, 0};
+    unsigned long long tests = 0;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const uint64_t c = c_warp + (uint64_t)r * 128 + lane * 4;
+        unsigned long long run = base + row_excl[r];
+        uint32_t st[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            st[k] = (uint32_t)run;
+            run += v[4 * r + k];
+            const int cl = list_of(v[4 * r + k]);
+            if (cl >= 0) my_cls[cl]++;
+            tests += (unsigned long long)v[4 * r + k] * (v[4 * r + k] - (v[4 * r + k] ? 1u : 0u)) / 2;
+        }
+        if (full) {
+            *reinterpret_cast<uint4*>(p.starts + c) = make_uint4(st[0], st[1], st[2], st[3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (c + k < p.ncells) p.starts[c + k] = st[k];
+        }
+    }
+    // tile end: the last tile writes starts[ncells] and the entry total
+    if (t == 0 && (tile + 1) * kScanTile >= p.ncells) {
+        const unsigned long long total = s_prefix + agg;
+        p.starts[p.ncells] = (uint32_t)total;
+        p.ctr->entries = total;
+        if (total >= (1ull << 32)) atomicOr(&p.ctr->err, kErrEntryOvf);
+    }
+    tests = warp_sum_u64(tests);
+    if (lane == 0 && tests) atomicAdd(&s_tests, tests);
+#pragma unroll
+    for (int c = 0; c < kNumLists; c++)
+        if (my_cls[c]) atomicAdd(&s_cls[c], my_cls[c]);
+    __syncthreads();
+    if (t < kNumLists) {
+        s_cls_base[t] = s_cls[t] ? atomicAdd(&p.ctr->n_list[t], s_cls[t]) : 0u;
+        s_cls[t] = 0;
+    }
+    if (t == 0 && s_tests) atomicAdd(&p.ctr->tests, s_tests);
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const uint64_t c = c_warp + (uint64_t)r * 128 + lane * 4;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int cl = list_of(v[4 * r + k]);
+            if (cl >= 0) {
+                const uint64_t idx = (uint64_t)s_cls_base[cl] + atomicAdd(&s_cls[cl], 1u);
+                if (idx < p.list_cap[cl]) p.lists[p.list_off[cl] + idx] = (uint32_t)(c + k);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// expand: cells larger than kBigMax get tile tasks {cell, row tile r, column
+// tiles [x0,x1)} with 32-box tiles, x >= r, at most 8 column tiles a task.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kTaskCols = 8;
+
+__global__ void k_expand(Params p) {
+    const uint32_t nh = mn64(p.ctr->n_list[kListHuge], p.list_cap[kListHuge]);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nh; i += gridDim.x * blockDim.x) {
+        const uint32_t cell = p.lists[p.list_off[kListHuge] + i];
+        const uint32_t n = p.starts[cell + 1] - p.starts[cell];
+        const uint32_t R = (n + 31) >> 5;
+        uint32_t cnt = 0;
+        for (uint32_t r = 0; r < R; r++) cnt += (R - r + kTaskCols - 1) / kTaskCols;
+        const uint32_t b = atomicAdd(&p.ctr->need_tasks, cnt);
+        uint32_t k = 0;
+        for (uint32_t r = 0; r < R; r++)
+            for (uint32_t x0 = r; x0 < R; x0 += kTaskCols, k++)
+                if ((uint64_t)b + k < p.task_cap) p.tasks[b + k] = make_uint4(cell, r, x0, min(x0 + kTaskCols, R));
+        if ((uint64_t)b + cnt > p.task_cap) atomicOr(&p.ctr->err, kErrTaskOvf);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pair test
+// ---------------------------------------------------------------------------
+constexpr int kPairThreads = 256;
+constexpr int kPairWarps = kPairThreads / 32;
+constexpr uint32_t kSlots = kBigMax;       // staged boxes per block (32 B each)
+constexpr uint32_t kOutBuf = 4096;         // block output buffer (pairs)
+constexpr uint32_t kFlushAt = 2048;
+constexpr uint32_t kBigCellsPerTask = 16;
+
+struct Box {
+    uint32_t x0, x1, y0, y1, z0, z1, f, id;
+};
+
+struct PairSmem {
+    uint4 a[kSlots];        // x0 x1 y0 y1
+    uint4 b[kSlots];        // z0 z1 flags id
+    uint2 out[kOutBuf];
+    uint32_t out_n, first_ovf;
+    unsigned long long gbase;
+    uint32_t cell_start[kBigCellsPerTask], cell_n[kBigCellsPerTask], cell_off[kBigCellsPerTask + 1];
+    uint32_t unit_pref[kBigCellsPerTask + 1];
+    uint32_t k, tot, units;
+    unsigned long long nbt[kNumLists];
+};
+
+__device__ __forceinline__ void slot_put(PairSmem& s, uint32_t i, const Box& x) {
+    s.a[i] = make_uint4(x.x0, x.x1, x.y0, x.y1);
+    s.b[i] = make_uint4(x.z0, x.z1, x.f, x.id);
+}
+__device__ __forceinline__ Box slot_get(const PairSmem& s, uint32_t i) {
+    const uint4 a = s.a[i], b = s.b[i];
+    Box x;
+    x.x0 = a.x; x.x1 = a.y; x.y0 = a.z; x.y1 = a.w;
+    x.z0 = b.x; x.z1 = b.y; x.f = b.z; x.id = b.w;
+    return x;
+}
+__device__ __forceinline__ uint32_t slot_id(const PairSmem& s, uint32_t i) { return s.b[i].w; }
+
+template <int D>
+__device__ __forceinline__ Box load_entry(const Params& p, uint32_t raw) {
+    Box x;
+    x.id = raw & kIdMask;
+    x.f = raw >> kIdBits;
+    if (x.id >= p.nboxes) {  // cannot happen with a consistent grid; never read past the boxes
+        atomicOr(&p.ctr->err, kErrIndex);
+        x.x0 = x.y0 = x.z0 = 1u; x.x1 = x.y1 = x.z1 = 0u; x.f = 0;
+        return x;
+    }
+    const uint32_t* b = p.boxes + (uint64_t)x.id * (2 * D + 1);
+    x.x0 = __ldg(b); x.x1 = __ldg(b + 1); x.y0 = __ldg(b + 2); x.y1 = __ldg(b + 3);
+    if (D == 3) { x.z0 = __ldg(b + 4); x.z1 = __ldg(b + 5); }
+    else { x.z0 = 0; x.z1 = 0; }
+    return x;
+}
+
+// closed-interval overlap on every axis (calcOverlaps, pbig.cu:562-577) and
+// the reference-cell rule (calcRightToWrite, pbig.cu:579-603) via flags
+template <int D, bool BIP>
+__device__ __forceinline__ bool hit(const Box& a, const Box& b, uint32_t split) {
+    bool ok = (a.x0 <= b.x1) & (b.x0 <= a.x1) & (a.y0 <= b.y1) & (b.y0 <= a.y1) & ((a.f | b.f) == 7u);
+    if (D == 3) ok = ok & (a.z0 <= b.z1) & (b.z0 <= a.z1);
+    if (BIP) ok = ok & ((a.id < split) != (b.id < split));
+    return ok;
+}
+
+// warp-wide compaction of the set bits of `mask` into the block buffer
+// (ballot/popc ranks and one shared-memory reservation per warp); when the
+// buffer is full the warp reserves global space itself.
+template <bool BIP, class PartnerId>
+__device__ __forceinline__ void emit(const Params& p, PairSmem& s, uint32_t mask, uint32_t myid,
+                                     PartnerId pid) {
+    const uint32_t lane = lane_id();
+    const uint32_t k = __popc(mask);
+    const uint32_t incl = warp_incl_scan(k);
+    const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+    if (total == 0) return;
+    uint32_t pos = 0;
+    unsigned long long gbase = 0;
+    if (lane == 0) {
+        pos = atomicAdd(&s.out_n, total);
+        if (pos + total > kOutBuf) {
+            atomicMin(&s.first_ovf, pos);
+            gbase = atomicAdd(&p.ctr->pairs, (unsigned long long)total);
+        }
+    }
+    pos = __shfl_sync(FULL_MASK, pos, 0);
+    gbase = __shfl_sync(FULL_MASK, gbase, 0);
+    const bool direct = pos + total > kOutBuf;
+    uint32_t w = incl - k;
+    while (mask) {
+        const int bit = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const uint32_t q = pid(bit);
+        uint2 pr = make_uint2(min(myid, q), max(myid, q));
+        if (BIP) pr.y -= p.split;
+        if (!direct) {
+            s.out[pos + w] = pr;
+        } else {
+            const unsigned long long g = gbase + w;
+            if (g < p.out_cap) p.out[g] = pr;
+            else atomicOr(&p.ctr->err, kErrOutOvf);
+        }
+        w++;
+    }
+}
+
+// cells of at most WG boxes, 32/WG cells per warp, lane r of a group holds
+// box r and tests it against the next floor(n/2) boxes of the cell
+// circularly (the BALANCE=1 sweep of d_matching, pbig.cu:804-825), so every
+// unordered pair of the cell is tested exactly once.
+template <int D, int WG, bool BIP>
+__device__ __forceinline__ void small_item(const Params& p, PairSmem& s, int list, uint64_t item,
+                                           uint32_t slot0) {
+    constexpr uint32_t G = 32 / WG;
+    const uint32_t lane = lane_id(), g = lane / WG, r = lane % WG;
+    const uint64_t ci = item * G + g;
+    const uint64_t nl = mn64(p.ctr->n_list[list], p.list_cap[list]);
+    uint32_t n = 0, start = 0;
+    if (ci < nl) {
+        const uint32_t cell = p.lists[p.list_off[list] + ci];
+        start = p.starts[cell];
+        n = p.starts[cell + 1] - start;
+        if (n > WG || (uint64_t)start + n > p.entry_cap) n = 0;  // inconsistent grid: skip
+    }
+    const bool have = r < n;
+    Box me;
+    if (have) {
+        me = load_entry<D>(p, p.entries[start + r]);
+        slot_put(s, slot0 + lane, me);
+    }
+    __syncwarp();
+    const uint32_t nelm = have ? (r < (n >> 1) ? (n >> 1) : ((n - 1) >> 1)) : 0u;
+    uint32_t mask = 0;
+    const uint32_t gb = slot0 + g * WG;
+#pragma unroll
+    for (uint32_t d = 1; d <= WG / 2; d++) {
+        if (d <= nelm) {
+            uint32_t pr = r + d;
+            if (pr >= n) pr -= n;
+            if (hit<D, BIP>(me, slot_get(s, gb + pr), p.split)) mask |= 1u << d;
+        }
+    }
+    emit<BIP>(p, s, mask, have ? me.id : 0u, [&](int d) {
+        uint32_t pr = r + (uint32_t)d;
+        if (pr >= n) pr -= n;
+        return slot_id(s, gb + pr);
+    });
+    __syncwarp();
+}
+
+// one 32x32 tile unit of a staged cell: rows = boxes [32r, 32r+32) of the
+// cell, columns = boxes [32x, 32x+32); x == r is the diagonal tile (circular
+// sweep), x > r a full rectangle with the column box broadcast to all lanes.
+template <int D, bool BIP>
+__device__ __forceinline__ void tile_unit(const Params& p, PairSmem& s, uint32_t row_slot0, uint32_t col_slot0,
+                                          uint32_t rows, uint32_t cols, bool diag) {
+    const uint32_t lane = lane_id();
+    const bool have = lane < rows;
+    Box me;
+    if (have) me = slot_get(s, row_slot0 + lane);
+    uint32_t mask = 0;
+    if (diag) {
+        const uint32_t nelm = have ? (lane < (rows >> 1) ? (rows >> 1) : ((rows - 1) >> 1)) : 0u;
+#pragma unroll
+        for (uint32_t d = 1; d <= 16; d++) {
+            if (d <= nelm) {
+                uint32_t pr = lane + d;
+                if (pr >= rows) pr -= rows;
+                if (hit<D, BIP>(me, slot_get(s, row_slot0 + pr), p.split)) mask |= 1u << d;
+            }
+        }
+        emit<BIP>(p, s, mask, have ? me.id : 0u, [&](int d) {
+            uint32_t pr = lane + (uint32_t)d;
+            if (pr >= rows) pr -= rows;
+            return slot_id(s, row_slot0 + pr);
+        });
+    } else {
+        if (have) {
+            if (cols == 32) {
+#pragma unroll
+                for (uint32_t j = 0; j < 32; j++)
+                    if (hit<D, BIP>(me, slot_get(s, col_slot0 + j), p.split)) mask |= 1u << j;
+            } else {
+                for (uint32_t j = 0; j < cols; j++)
+                    if (hit<D, BIP>(me, slot_get(s, col_slot0 + j), p.split)) mask |= 1u << j;
+            }
+        }
+        emit<BIP>(p, s, mask, have ? me.id : 0u, [&](int j) { return slot_id(s, col_slot0 + (uint32_t)j); });
+    }
+}
+
+// cells of 33..kBigMax boxes: up to kBigCellsPerTask cells are staged whole
+// into shared memory (as many as fit), then the block's warps share their
+// 32x32 tile units.
+template <int D, bool BIP>
+__device__ void big_task(const Params& p, PairSmem& s, uint64_t task) {
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    const uint64_t nl = mn64(p.ctr->n_list[kListBig], p.list_cap[kListBig]);
+    uint64_t cur = task * kBigCellsPerTask;
+    const uint64_t end = mn64(cur + kBigCellsPerTask, nl);
+    while (cur < end) {
+        if (warp == 0) {
+            uint32_t n = 0, st = 0;
+            const bool v = lane < kBigCellsPerTask && cur + lane < end;
+            if (v) {
+                const uint32_t cell = p.lists[p.list_off[kListBig] + cur + lane];
+                st = p.starts[cell];
+                n = p.starts[cell + 1] - st;
+                if (n > kBigMax || (uint64_t)st + n > p.entry_cap) n = 0;  // inconsistent grid: skip
+            }
+            const uint32_t inc = warp_incl_scan(n);
+            const uint32_t fits = __ballot_sync(FULL_MASK, v && inc <= kSlots);
+            const uint32_t k = __popc(fits);  // prefix property: fits is a low-bit run
+            const uint32_t R = (n + 31) >> 5;
+            const uint32_t u = (v && lane < k) ? R * (R + 1) / 2 : 0u;
+            const uint32_t uinc = warp_incl_scan(u);
+            if (lane < k) {
+                s.cell_start[lane] = st;
+                s.cell_n[lane] = n;
+                s.cell_off[lane] = inc - n;
+                s.unit_pref[lane + 1] = uinc;
+            }
+            if (lane == 0) s.unit_pref[0] = 0;
+            if (lane == 0 && k == 0) {
+                s.k = 0;
+                s.tot = 0;
+                s.units = 0;
+            }
+            if (lane == k - 1) {
+                s.cell_off[k] = inc;
+                s.k = k;
+                s.tot = inc;
+                s.units = uinc;
+            }
+        }
+        __syncthreads();
+        const uint32_t K = s.k, tot = s.tot, U = s.units;
+        if (K == 0) break;  // uniform: every thread read the same K
+        for (uint32_t e = t; e < tot; e += kPairThreads) {
+            uint32_t c = 0;
+            while (c + 1 < K && s.cell_off[c + 1] <= e) c++;
+            slot_put(s, e, load_entry<D>(p, p.entries[s.cell_start[c] + (e - s.cell_off[c])]));
+        }
+        __syncthreads();
+        for (uint32_t u = warp; u < U; u += kPairWarps) {
+            uint32_t c = 0;
+            while (c + 1 < K && s.unit_pref[c + 1] <= u) c++;
+            uint32_t lu = u - s.unit_pref[c];
+            const uint32_t n = s.cell_n[c], off = s.cell_off[c], R = (n + 31) >> 5;
+            uint32_t r = 0;
+            while (lu >= R - r) { lu -= R - r; r++; }
+            const uint32_t x = r + lu;
+            tile_unit<D, BIP>(p, s, off + 32 * r, off + 32 * x, min(32u, n - 32 * r), min(32u, n - 32 * x), x == r);
+        }
+        __syncthreads();
+        cur += K;
+    }
+}
+
+// cells larger than kBigMax: one tile task per warp, boxes gathered per tile
+template <int D, bool BIP>
+__device__ __forceinline__ void huge_item(const Params& p, PairSmem& s, uint64_t item, uint32_t slot0) {
+    const uint32_t lane = lane_id();
+    const uint64_t nt = mn64(p.ctr->need_tasks, p.task_cap);
+    if (item >= nt) return;
+    const uint4 tk = p.tasks[item];
+    const uint32_t cell = tk.x, r = tk.y, x0 = tk.z, x1 = tk.w;
+    const uint32_t start = p.starts[cell], n = p.starts[cell + 1] - start;
+    if ((uint64_t)start + n > p.entry_cap || 32ull * r >= n || 32ull * (x1 - 1) >= n) return;
+    const uint32_t rows = min(32u, n - 32 * r);
+    if (lane < rows) slot_put(s, slot0 + lane, load_entry<D>(p, p.entries[start + 32 * r + lane]));
+    __syncwarp();
+    for (uint32_t x = x0; x < x1; x++) {
+        const uint32_t cols = min(32u, n - 32 * x);
+        if (x != r) {
+            if (lane < cols) slot_put(s, slot0 + 32 + lane, load_entry<D>(p, p.entries[start + 32 * x + lane]));
+            __syncwarp();
+        }
+        tile_unit<D, BIP>(p, s, slot0, slot0 + 32, rows, cols, x == r);
+        __syncwarp();
+    }
+}
+
+template <int D, bool BIP>
+__global__ void __launch_bounds__(kPairThreads, 4) k_pairs(Params p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PairSmem& s = *reinterpret_cast<PairSmem*>(smem_raw);
+    const uint32_t t = threadIdx.x, warp = t >> 5;
+    if (t == 0) {
+        s.out_n = 0;
+        s.first_ovf = kOutBuf;
+    }
+    // block-task space: [small classes][big groups][huge tile tasks]
+    if (t < kNumLists) {
+        uint64_t nl;
+        uint32_t per;
+        if (t < 4) {
+            nl = mn64(p.ctr->n_list[t], p.list_cap[t]);
+            per = kPairWarps * (32u >> (2 + t));  // warps x cells per warp (WG = 4,8,16,32)
+        } else if (t == kListBig) {
+            nl = mn64(p.ctr->n_list[kListBig], p.list_cap[kListBig]);
+            per = kBigCellsPerTask;
+        } else {
+            nl = mn64(p.ctr->need_tasks, p.task_cap);
+            per = kPairWarps;
+        }
+        s.nbt[t] = (nl + per - 1) / per;
+    }
+    __syncthreads();
+    uint64_t total = 0;
+#pragma unroll
+    for (int c = 0; c < kNumLists; c++) total += s.nbt[c];
+    const uint32_t slot0 = warp * 64;
+    for (uint64_t bt = blockIdx.x; bt < total; bt += gridDim.x) {
+        uint64_t rem = bt;
+        int cls = 0;
+        while (cls < kNumLists - 1 && rem >= s.nbt[cls]) { rem -= s.nbt[cls]; cls++; }
+        switch (cls) {
+            case 0: small_item<D, 4, BIP>(p, s, 0, rem * kPairWarps + warp, slot0); break;
+            case 1: small_item<D, 8, BIP>(p, s, 1, rem * kPairWarps + warp, slot0); break;
+            case 2: small_item<D, 16, BIP>(p, s, 2, rem * kPairWarps + warp, slot0); break;
+            case 3: small_item<D, 32, BIP>(p, s, 3, rem * kPairWarps + warp, slot0); break;
+            case kListBig: big_task<D, BIP>(p, s, rem); break;
+            default: huge_item<D, BIP>(p, s, rem * kPairWarps + warp, slot0); break;
+        }
+        __syncthreads();
+        const uint32_t on = s.out_n, ovf = s.first_ovf;
+        const uint32_t nv = min(on, ovf);
+        const bool last = bt + gridDim.x >= total;
+        if (nv >= kFlushAt || on > nv || (last && on > 0)) {
+            if (t == 0) s.gbase = nv ? atomicAdd(&p.ctr->pairs, (unsigned long long)nv) : 0ull;
+            __syncthreads();
+            const unsigned long long gb = s.gbase;
+            for (uint32_t k = t; k < nv; k += kPairThreads) {
+                const unsigned long long g = gb + k;
+                if (g < p.out_cap) p.out[g] = s.out[k];
+                else atomicOr(&p.ctr->err, kErrOutOvf);
+            }
+            __syncthreads();
+            if (t == 0) {
+                s.out_n = 0;
+                s.first_ovf = kOutBuf;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// group pairs by scene (batched queries): a pair's scene is the scene of its
+// first box; pairs are written to their scene's range with scene-local ids.
+// ---------------------------------------------------------------------------
+__global__ void k_group_by_scene(Params p, const unsigned long long* scene_pair_off,
+                                 unsigned long long* scene_cursor, uint2* dst, unsigned long long n) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint2 pr = p.out[i];
+        const uint32_t sc = find_scene(p, pr.x);
+        const uint32_t off = p.scene_box_off[sc];
+        const unsigned long long k = atomicAdd(&scene_cursor[sc], 1ull);
+        dst[scene_pair_off[sc] + k] = make_uint2(pr.x - off, pr.y - off);
+    }
+}
+
+__global__ void k_scene_hist(Params p, unsigned long long* hist, unsigned long long n) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t sc = find_scene(p, p.out[i].x);
+        atomicAdd(&hist[sc], 1ull);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static int g_pair_blocks_per_sm = 0;
+
+size_t pair_smem_bytes() { return sizeof(PairSmem); }
+
+cudaError_t kernels_init() {
+    const int sm = (int)sizeof(PairSmem);
+    cudaError_t e;
+#define SET_SMEM(K)                                                                             \
+    e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);               \
+    if (e != cudaSuccess) return e;
+    SET_SMEM((k_pairs<2, false>));
+    SET_SMEM((k_pairs<3, false>));
+    SET_SMEM((k_pairs<2, true>));
+    SET_SMEM((k_pairs<3, true>));
+#undef SET_SMEM
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs<3, false>, kPairThreads, sm);
+    if (e != cudaSuccess) return e;
+    g_pair_blocks_per_sm = nb > 0 ? nb : 1;
+    return cudaSuccess;
+}
+
+int pair_blocks_per_sm() { return g_pair_blocks_per_sm > 0 ? g_pair_blocks_per_sm : 1; }
+
+cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st) {
+    const unsigned long long n = p.out_cap;
+    if (n == 0) return cudaSuccess;
+    const unsigned long long blocks = mn64((n + 255) / 256, 152ull * 16);
+    k_scene_hist<<<(unsigned)blocks, 256, 0, st>>>(p, hist, n);
+    return cudaGetLastError();
+}
+
+uint64_t scan_tiles(uint64_t ncells) { return (ncells + kScanTile - 1) / kScanTile; }
+
+cudaError_t launch_count(const Params& p, int dims, cudaStream_t st) {
+    const uint64_t nb = (p.nboxes + kBoxThreads - 1) / kBoxThreads;
+    if (nb == 0) return cudaSuccess;
+    if (dims == 2) k_count<2><<<(unsigned)nb, kBoxThreads, 0, st>>>(p);
+    else k_count<3><<<(unsigned)nb, kBoxThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st) {
+    const uint64_t nb = (p.nboxes + kBoxThreads - 1) / kBoxThreads;
+    if (nb == 0) return cudaSuccess;
+    if (dims == 2) k_scatter<2><<<(unsigned)nb, kBoxThreads, 0, st>>>(p);
+    else k_scatter<3><<<(unsigned)nb, kBoxThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan(const Params& p, cudaStream_t st) {
+    const uint64_t tiles = scan_tiles(p.ncells);
+    k_scan<<<(unsigned)tiles, kScanThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_expand(const Params& p, cudaStream_t st) {
+    k_expand<<<64, 256, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pairs(const Params& p, int dims, int grid_blocks, cudaStream_t st) {
+    const size_t sm = sizeof(PairSmem);
+    const bool bip = p.split != kNoSplit;
+    if (dims == 2) {
+        if (bip) k_pairs<2, true><<<grid_blocks, kPairThreads, sm, st>>>(p);
+        else k_pairs<2, false><<<grid_blocks, kPairThreads, sm, st>>>(p);
+    } else {
+        if (bip) k_pairs<3, true><<<grid_blocks, kPairThreads, sm, st>>>(p);
+        else k_pairs<3, false><<<grid_blocks, kPairThreads, sm, st>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,
+                                  unsigned long long* scene_cursor, uint2* dst, cudaStream_t st) {
+    // pair count is read on the host before this launch; p.out_cap carries it
+    const unsigned long long n = p.out_cap;
+    if (n == 0) return cudaSuccess;
+    const unsigned long long blocks = mn64((n + 255) / 256, 152ull * 16);
+    k_group_by_scene<<<(unsigned)blocks, 256, 0, st>>>(p, scene_pair_off, scene_cursor, dst, n);
+    return cudaGetLastError();
+}
+
+}  // namespace pbig

@@ -1,0 +1,93 @@
+// Device-side data structures and kernel launchers of the pair-detection
+// pipeline (count -> scan -> expand -> scatter -> pair test).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pbig {
+
+// error bits accumulated in Ctr::err
+enum : uint32_t {
+    kErrRange = 1u,       // a coordinate >= range
+    kErrInverted = 2u,    // min > max on some axis
+    kErrRid = 4u,         // rid != index within the scene
+    kErrEntryOvf = 8u,    // entry buffer too small (E > capacity)
+    kErrOutOvf = 16u,     // pair buffer too small
+    kErrWait = 32u,       // a bounded spin-wait gave up
+    kErrTaskOvf = 64u,    // tile-task buffer too small
+    kErrCellOvf = 128u,   // one box covers >= 2^31 cells
+    kErrIndex = 256u      // more than 2^29 boxes in one launch
+};
+
+constexpr uint32_t kNoSplit = 0xffffffffu;
+constexpr int kIdBits = 29;
+constexpr uint32_t kIdMask = (1u << kIdBits) - 1u;
+
+// class lists built by the scan: cells with 2..4, 5..8, 9..16, 17..32 boxes
+// (warp-packed), 33..kBigMax (block-staged) and larger (tiled)
+constexpr int kNumLists = 6;
+constexpr int kListBig = 4, kListHuge = 5;
+constexpr uint32_t kBigMax = 512;   // largest cell staged whole in shared memory
+
+struct Scene {
+    uint32_t box_off;   // first box of the scene (global index)
+    uint32_t n;         // boxes in the scene
+    uint32_t shift;     // log2(cell size)
+    uint32_t nrc;       // cells per axis: ceil(range / 2^shift)
+    uint64_t cell_off;  // first cell of the scene's grid (global cell id)
+    uint32_t range;     // coordinate bound
+    uint32_t pad;
+};
+
+// device-resident counters of one run (zeroed before the run)
+struct Ctr {
+    unsigned int err;
+    unsigned int bad;
+    unsigned int ticket;                // scan tile ticket
+    unsigned int n_list[kNumLists];     // class list sizes
+    unsigned int n_tasks;               // tile tasks written for huge cells
+    unsigned int need_tasks;            // tile tasks needed
+    unsigned int pad;
+    unsigned long long entries;         // E
+    unsigned long long pairs;           // pairs found (may exceed capacity)
+    unsigned long long tests;           // sum of n(n-1)/2 over cells
+};
+
+struct Params {
+    const uint32_t* boxes;        // RectInfo records, 2*D+1 words each
+    uint64_t nboxes;              // boxes over all scenes
+    const Scene* scenes;          // scene table (device)
+    const uint32_t* scene_box_off;// nscenes+1 box offsets (device)
+    uint32_t nscenes;
+    uint32_t split;               // bipartite: global index of the first blue box
+    uint32_t* counts;             // [ncells] (zero before count; zero after scatter)
+    uint32_t* starts;             // [ncells+1] exclusive scan of counts
+    uint64_t ncells;
+    uint32_t* entries;            // [entry_cap]: flags<<29 | global box index
+    uint64_t entry_cap;
+    uint32_t* lists;              // kNumLists regions
+    uint64_t list_off[kNumLists]; // region offsets into lists
+    uint64_t list_cap[kNumLists];
+    uint4* tasks;                 // huge-cell tile tasks {cell, r, x0, x1}
+    uint64_t task_cap;
+    unsigned long long* tile_state; // scan look-back state, one per tile
+    uint2* out;                   // pairs
+    uint64_t out_cap;
+    Ctr* ctr;
+};
+
+// launchers (all asynchronous on `st`); dims is 2 or 3
+cudaError_t launch_count(const Params& p, int dims, cudaStream_t st);
+cudaError_t launch_scan(const Params& p, cudaStream_t st);
+cudaError_t launch_expand(const Params& p, cudaStream_t st);
+cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st);
+cudaError_t launch_pairs(const Params& p, int dims, int grid_blocks, cudaStream_t st);
+cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,
+                                  unsigned long long* scene_cursor, uint2* dst, cudaStream_t st);
+cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st);
+uint64_t scan_tiles(uint64_t ncells);
+int pair_blocks_per_sm();
+size_t pair_smem_bytes();
+cudaError_t kernels_init();
+
+}  // namespace pbig

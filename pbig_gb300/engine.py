@@ -1,0 +1,242 @@
+"""Python face of the C ABI (``include/pbig2.h``), via ctypes.
+
+``Engine`` mirrors the reference's ``pbig_init`` / ``pbig_check`` /
+``pbig_finalize`` life cycle (src/pbig/pbig.cu:2139, 1962, 141 of awatch/pbig)
+with explicit results instead of a callback: a query returns the number of
+overlapping pairs and the pairs stay on the device until the next query.
+
+Inputs are PBIG ``RectInfo`` rows (uint32, 5 words in 2-D, 7 in 3-D, rid =
+row index): a numpy array (host memory) or a CUDA tensor (device memory;
+int32 or uint32, same bit pattern). There is no CPU fallback: without the
+CUDA library or a GPU the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native
+
+OK, EINVAL, ENOMEM, ECUDA, EINPUT, ETIMEOUT, ECAPACITY, EBUSY = range(8)
+HOST, DEVICE = 0, 1
+AUTO = 0xFFFFFFFF
+
+EXPORTS = [
+    "pbig2_create", "pbig2_destroy", "pbig2_last_error", "pbig2_version", "pbig2_self_intersect",
+    "pbig2_bipartite_intersect", "pbig2_batch_intersect", "pbig2_result_pairs", "pbig2_copy_pairs",
+    "pbig2_result_scene_offsets", "pbig2_copy_pairs_async", "pbig2_sync", "pbig2_host_alloc",
+    "pbig2_host_free", "pbig2_get_stats", "pbig2_tune_shift",
+]
+
+
+class PbigError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"pbig2 error {code}: {msg}")
+        self.code = code
+
+
+class Stats(C.Structure):
+    _fields_ = [("boxes", C.c_uint64), ("bad_boxes", C.c_uint64), ("cells", C.c_uint64),
+                ("entries", C.c_uint64), ("pair_tests", C.c_uint64), ("pairs", C.c_uint64),
+                ("cell_shift", C.c_uint32), ("scenes", C.c_uint32), ("kernels", C.c_uint32),
+                ("reserved", C.c_uint32), ("device_ms", C.c_double), ("phase_ms", C.c_double * 6)]
+
+    PHASES = ("count", "scan", "expand", "scatter", "pairs", "group")
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "phase_ms")}
+        d["phase_ms"] = dict(zip(self.PHASES, list(self.phase_ms)))
+        return d
+
+
+_LIB = None
+
+
+def lib():
+    """The loaded engine library (built in-tree on first use)."""
+    global _LIB
+    if _LIB is None:
+        L = C.CDLL(_native.lib_path("engine"))
+        vp, u64, u32 = C.c_void_p, C.c_uint64, C.c_uint32
+        L.pbig2_create.argtypes = [C.c_int, C.POINTER(vp)]
+        L.pbig2_destroy.argtypes = [vp]
+        L.pbig2_last_error.restype = C.c_char_p
+        L.pbig2_self_intersect.argtypes = [vp, vp, u64, u32, u32, u32, C.c_int, vp, C.POINTER(u64)]
+        L.pbig2_bipartite_intersect.argtypes = [vp, vp, u64, vp, u64, u32, u32, u32, C.c_int, vp,
+                                                C.POINTER(u64)]
+        L.pbig2_batch_intersect.argtypes = [vp, vp, C.POINTER(u64), u32, u32, u32, vp, C.c_int, vp,
+                                            C.POINTER(u64)]
+        L.pbig2_result_pairs.argtypes = [vp, C.POINTER(vp), C.POINTER(u64)]
+        L.pbig2_copy_pairs.argtypes = [vp, vp, u64, u64, C.c_int, vp]
+        L.pbig2_copy_pairs_async.argtypes = [vp, vp, u64, u64, C.c_int, vp]
+        L.pbig2_sync.argtypes = [vp, vp]
+        L.pbig2_result_scene_offsets.argtypes = [vp, C.POINTER(u64), u32]
+        L.pbig2_get_stats.argtypes = [vp, C.POINTER(Stats)]
+        L.pbig2_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
+        L.pbig2_host_free.argtypes = [vp]
+        L.pbig2_tune_shift.argtypes = [vp, u64, u32, u32, u64, C.POINTER(u32)]
+        _LIB = L
+    return _LIB
+
+
+def _check(rc: int, allow=(OK,)) -> int:
+    if rc not in allow:
+        raise PbigError(rc, lib().pbig2_last_error().decode())
+    return rc
+
+
+def _boxes_arg(boxes):
+    """(pointer, n rows, dims, location, keepalive) for a numpy array or a
+    CUDA tensor of RectInfo rows."""
+    if isinstance(boxes, np.ndarray):
+        a = np.ascontiguousarray(boxes, dtype=np.uint32)
+        if a.ndim != 2 or a.shape[1] not in (5, 7):
+            raise ValueError("boxes must be [n,5] (2-D) or [n,7] (3-D) RectInfo rows")
+        return a.ctypes.data, a.shape[0], (a.shape[1] - 1) // 2, HOST, a
+    import torch
+    t = boxes
+    if not isinstance(t, torch.Tensor):
+        raise TypeError("boxes must be a numpy array or a torch tensor")
+    if t.dim() != 2 or t.shape[1] not in (5, 7) or t.element_size() != 4 or not t.is_contiguous():
+        raise ValueError("boxes tensor must be contiguous [n,5] or [n,7] with 4-byte elements")
+    loc = DEVICE if t.is_cuda else HOST
+    return t.data_ptr(), t.shape[0], (t.shape[1] - 1) // 2, loc, t
+
+
+@dataclass
+class Result:
+    npairs: int
+    rc: int
+
+
+class Engine:
+    """One CUDA device, its buffers and stream (not thread-safe)."""
+
+    def __init__(self, device: int = 0):
+        self._L = lib()
+        ctx = C.c_void_p()
+        _check(self._L.pbig2_create(device, C.byref(ctx)))
+        self._ctx = ctx
+        self.device = device
+        self.last_rc = OK
+        self._keep = None
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.pbig2_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @staticmethod
+    def _stream(stream):
+        if stream is None:
+            return None
+        return C.c_void_p(getattr(stream, "cuda_stream", stream))
+
+    def self_intersect(self, boxes, range_: int, cell_shift: int | None = None, stream=None,
+                       allow_bad: bool = False) -> int:
+        """All overlapping pairs of one scene; returns the pair count."""
+        ptr, n, dims, loc, keep = _boxes_arg(boxes)
+        self._keep = keep
+        out = C.c_uint64()
+        rc = self._L.pbig2_self_intersect(self._ctx, C.c_void_p(ptr), n, dims, range_,
+                                          AUTO if cell_shift is None else cell_shift, loc,
+                                          self._stream(stream), C.byref(out))
+        self.last_rc = _check(rc, (OK, EINPUT) if allow_bad else (OK,))
+        return out.value
+
+    def bipartite_intersect(self, red, blue, range_: int, cell_shift: int | None = None, stream=None) -> int:
+        """Pairs (red index, blue index) of overlapping red/blue boxes."""
+        pr, nr, dr, lr, kr = _boxes_arg(red)
+        pb, nb, db, lb, kb = _boxes_arg(blue)
+        if dr != db or lr != lb:
+            raise ValueError("red and blue must have the same dims and memory location")
+        self._keep = (kr, kb)
+        out = C.c_uint64()
+        rc = self._L.pbig2_bipartite_intersect(self._ctx, C.c_void_p(pr), nr, C.c_void_p(pb), nb, dr, range_,
+                                               AUTO if cell_shift is None else cell_shift, lr,
+                                               self._stream(stream), C.byref(out))
+        self.last_rc = _check(rc)
+        return out.value
+
+    def batch_intersect(self, boxes, scene_offsets, range_: int, cell_shifts=None, stream=None) -> int:
+        """Independent scenes (concatenated boxes, scene_offsets[n_scenes+1])."""
+        ptr, n, dims, loc, keep = _boxes_arg(boxes)
+        offs = np.ascontiguousarray(scene_offsets, dtype=np.uint64)
+        ns = offs.shape[0] - 1
+        if ns < 1 or int(offs[-1]) != n:
+            raise ValueError("scene_offsets must end at the number of boxes")
+        sh = None
+        if cell_shifts is not None:
+            sh = np.ascontiguousarray(cell_shifts, dtype=np.uint32)
+        self._keep = (keep, offs, sh)
+        out = C.c_uint64()
+        rc = self._L.pbig2_batch_intersect(self._ctx, C.c_void_p(ptr),
+                                           offs.ctypes.data_as(C.POINTER(C.c_uint64)), ns, dims, range_,
+                                           None if sh is None else C.c_void_p(sh.ctypes.data), loc,
+                                           self._stream(stream), C.byref(out))
+        self.last_rc = _check(rc)
+        self._nscenes = ns
+        return out.value
+
+    def scene_offsets(self) -> np.ndarray:
+        ns = self._nscenes
+        out = np.empty(ns + 1, dtype=np.uint64)
+        _check(self._L.pbig2_result_scene_offsets(self._ctx, out.ctypes.data_as(C.POINTER(C.c_uint64)), ns))
+        return out
+
+    def pairs(self, first: int = 0, count: int | None = None) -> np.ndarray:
+        """Pairs of the last query as a host [P,2] uint32 array."""
+        n = self.result_count()
+        count = n - first if count is None else count
+        out = np.empty((count, 2), dtype=np.uint32)
+        _check(self._L.pbig2_copy_pairs(self._ctx, C.c_void_p(out.ctypes.data), first, count, HOST, None))
+        return out
+
+    def pairs_into(self, dst, first: int = 0, stream=None) -> None:
+        """Copy the result into a preallocated host (pinned or not) or device
+        buffer: a tensor/array of shape [P,2] with 4-byte elements."""
+        if isinstance(dst, np.ndarray):
+            ptr, loc, count = dst.ctypes.data, HOST, dst.shape[0]
+        else:
+            ptr, loc, count = dst.data_ptr(), (DEVICE if dst.is_cuda else HOST), dst.shape[0]
+        _check(self._L.pbig2_copy_pairs_async(self._ctx, C.c_void_p(ptr), first, count, loc, self._stream(stream)))
+
+    def sync(self, stream=None):
+        _check(self._L.pbig2_sync(self._ctx, self._stream(stream)))
+
+    def device_pairs(self):
+        """(device pointer, count) of the resident result."""
+        p = C.c_void_p()
+        n = C.c_uint64()
+        _check(self._L.pbig2_result_pairs(self._ctx, C.byref(p), C.byref(n)))
+        return p.value, n.value
+
+    def result_count(self) -> int:
+        return self.device_pairs()[1]
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(self._L.pbig2_get_stats(self._ctx, C.byref(s)))
+        return s.as_dict()
+
+
+def tune_shift(boxes: np.ndarray, range_: int, sample: int = 4096) -> int:
+    a = np.ascontiguousarray(boxes, dtype=np.uint32)
+    out = C.c_uint32()
+    _check(lib().pbig2_tune_shift(C.c_void_p(a.ctypes.data), a.shape[0], (a.shape[1] - 1) // 2, range_, sample,
+                                  C.byref(out)))
+    return out.value
