@@ -54,6 +54,8 @@ def workload(name: str):
     from pbig_gb300 import gen
     if name == "clustered4m":
         return gen.clustered3d(4194304, seed=0), gen.RANGE, "3D self-intersection, 4,194,304 boxes, 64-Gaussian mixture (sigma 0.02), lognormal sides (median 0.002, log-sigma 0.5), seed 0"
+    if name == "clustered1m":
+        return gen.clustered3d(1048576, seed=0), gen.RANGE, "3D self-intersection, 1,048,576 boxes, 64-Gaussian mixture (sigma 0.02), lognormal sides (median 0.002, log-sigma 0.5), seed 0 (profiling size)"
     if name == "plain2d":
         return gen.uniform2d(65536, seed=0), gen.RANGE, "2D self-intersection, 65,536 boxes, uniform corners, sides U[0.001,0.005], seed 0"
     raise SystemExit(f"unknown workload {name}")
