@@ -286,6 +286,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     p.scene_box_off = c->d_scene_off.as<uint32_t>();
     p.nscenes = nsc;
     p.split = split;
+    p.max_range = range;
     p.ncells = ncells;
     p.tile_state = c->d_state.as<unsigned long long>();
     p.ctr = c->d_ctr.as<Ctr>();

@@ -367,21 +367,34 @@ __global__ void k_expand(Params p) {
 
 // ---------------------------------------------------------------------------
 // pair test
+//
+// Work classes (block tasks, static round robin over the grid):
+//   small  cells of 2..32 boxes, 32/WG cells per warp, circular half sweep
+//   big    cells of 33..kBigMax boxes: whole cells staged in shared memory,
+//          warps take row tiles (32 boxes) and sweep all column tiles
+//   huge   cells above kBigMax: tile tasks, boxes gathered per tile
+// The test of one (row box, column box) pair is branch free: with every
+// coordinate < 2^29 the six differences max-min are non-negative exactly
+// when the closed intervals overlap, and a negative difference sets bits
+// 29..31; the reference-cell rule adds the "does not start here" bits of
+// both boxes in bits 29..31, so the pair is reported iff the OR of all of
+// them is < 2^29. Wider coordinates use plain comparisons.
 // ---------------------------------------------------------------------------
 constexpr int kPairThreads = 256;
 constexpr int kPairWarps = kPairThreads / 32;
-constexpr uint32_t kSlots = kBigMax;       // staged boxes per block (32 B each)
+constexpr uint32_t kSlots = 1024;          // staged boxes per block (32 B each)
 constexpr uint32_t kOutBuf = 4096;         // block output buffer (pairs)
 constexpr uint32_t kFlushAt = 2048;
-constexpr uint32_t kBigCellsPerTask = 16;
+constexpr uint32_t kBigCellsPerTask = 32;
+constexpr uint32_t kMissShift = 29;
 
 struct Box {
-    uint32_t x0, x1, y0, y1, z0, z1, f, id;
+    uint32_t x0, x1, y0, y1, z0, z1, f, id;  // f: axes where the box does not start in this cell, << 29
 };
 
 struct PairSmem {
-    uint4 a[kSlots];        // x0 x1 y0 y1
-    uint4 b[kSlots];        // z0 z1 flags id
+    uint4 a[kSlots];  // x0 x1 y0 y1
+    uint4 b[kSlots];  // z0 z1 f id
     uint2 out[kOutBuf];
     uint32_t out_n, first_ovf;
     unsigned long long gbase;
@@ -404,15 +417,25 @@ __device__ __forceinline__ Box slot_get(const PairSmem& s, uint32_t i) {
 }
 __device__ __forceinline__ uint32_t slot_id(const PairSmem& s, uint32_t i) { return s.b[i].w; }
 
-template <int D>
+// a box that overlaps nothing (pads tiles to multiples of 8 and idle lanes)
+template <bool NARROW>
+__device__ __forceinline__ Box dummy_box() {
+    Box x;
+    x.x0 = x.y0 = x.z0 = NARROW ? (1u << 30) : 0xffffffffu;
+    x.x1 = x.y1 = x.z1 = 0u;
+    x.f = 7u << kMissShift;
+    x.id = 0;
+    return x;
+}
+
+template <int D, bool NARROW>
 __device__ __forceinline__ Box load_entry(const Params& p, uint32_t raw) {
     Box x;
     x.id = raw & kIdMask;
-    x.f = raw >> kIdBits;
+    x.f = (~(raw >> kIdBits) & 7u) << kMissShift;
     if (x.id >= p.nboxes) {  // cannot happen with a consistent grid; never read past the boxes
         atomicOr(&p.ctr->err, kErrIndex);
-        x.x0 = x.y0 = x.z0 = 1u; x.x1 = x.y1 = x.z1 = 0u; x.f = 0;
-        return x;
+        return dummy_box<NARROW>();
     }
     const uint32_t* b = p.boxes + (uint64_t)x.id * (2 * D + 1);
     x.x0 = __ldg(b); x.x1 = __ldg(b + 1); x.y0 = __ldg(b + 2); x.y1 = __ldg(b + 3);
@@ -422,23 +445,31 @@ __device__ __forceinline__ Box load_entry(const Params& p, uint32_t raw) {
 }
 
 // closed-interval overlap on every axis (calcOverlaps, pbig.cu:562-577) and
-// the reference-cell rule (calcRightToWrite, pbig.cu:579-603) via flags
-template <int D, bool BIP>
-__device__ __forceinline__ bool hit(const Box& a, const Box& b, uint32_t split) {
-    bool ok = (a.x0 <= b.x1) & (b.x0 <= a.x1) & (a.y0 <= b.y1) & (b.y0 <= a.y1) & ((a.f | b.f) == 7u);
-    if (D == 3) ok = ok & (a.z0 <= b.z1) & (b.z0 <= a.z1);
-    if (BIP) ok = ok & ((a.id < split) != (b.id < split));
+// the reference-cell rule (calcRightToWrite, pbig.cu:579-603); 1 or 0
+template <int D, bool BIP, bool NARROW>
+__device__ __forceinline__ uint32_t hit_bit(const Box& a, const Box& b, uint32_t split) {
+    uint32_t ok;
+    if (NARROW) {
+        uint32_t t = (b.x1 - a.x0) | (a.x1 - b.x0) | (b.y1 - a.y0) | (a.y1 - b.y0) | (a.f & b.f);
+        if (D == 3) t |= (b.z1 - a.z0) | (a.z1 - b.z0);
+        ok = t < (1u << kMissShift) ? 1u : 0u;
+    } else {
+        ok = ((a.x0 <= b.x1) & (b.x0 <= a.x1) & (a.y0 <= b.y1) & (b.y0 <= a.y1) & ((a.f & b.f) == 0u)) ? 1u : 0u;
+        if (D == 3) ok &= ((a.z0 <= b.z1) & (b.z0 <= a.z1)) ? 1u : 0u;
+    }
+    if (BIP) ok &= ((a.id < split) != (b.id < split)) ? 1u : 0u;
     return ok;
 }
 
-// warp-wide compaction of the set bits of `mask` into the block buffer
-// (ballot/popc ranks and one shared-memory reservation per warp); when the
-// buffer is full the warp reserves global space itself.
-template <bool BIP, class PartnerId>
-__device__ __forceinline__ void emit(const Params& p, PairSmem& s, uint32_t mask, uint32_t myid,
-                                     PartnerId pid) {
+// warp-wide compaction of the set bits of two masks into the block buffer
+// (ballot/popc-style ranks from one warp scan and one shared-memory
+// reservation per call); when the buffer is full the warp reserves global
+// space itself.
+template <bool BIP, class PA, class PB>
+__device__ __forceinline__ void emit2(const Params& p, PairSmem& s, uint32_t ma, PA pa, uint32_t mb, PB pb,
+                                      uint32_t myid) {
     const uint32_t lane = lane_id();
-    const uint32_t k = __popc(mask);
+    const uint32_t k = __popc(ma) + __popc(mb);
     const uint32_t incl = warp_incl_scan(k);
     const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
     if (total == 0) return;
@@ -455,10 +486,7 @@ __device__ __forceinline__ void emit(const Params& p, PairSmem& s, uint32_t mask
     gbase = __shfl_sync(FULL_MASK, gbase, 0);
     const bool direct = pos + total > kOutBuf;
     uint32_t w = incl - k;
-    while (mask) {
-        const int bit = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const uint32_t q = pid(bit);
+    auto put = [&](uint32_t q) {
         uint2 pr = make_uint2(min(myid, q), max(myid, q));
         if (BIP) pr.y -= p.split;
         if (!direct) {
@@ -469,14 +497,61 @@ __device__ __forceinline__ void emit(const Params& p, PairSmem& s, uint32_t mask
             else atomicOr(&p.ctr->err, kErrOutOvf);
         }
         w++;
+    };
+    while (ma) {
+        const uint32_t bit = __ffs(ma) - 1;
+        ma &= ma - 1;
+        put(pa(bit));
+    }
+    while (mb) {
+        const uint32_t bit = __ffs(mb) - 1;
+        mb &= mb - 1;
+        put(pb(bit));
     }
 }
 
-// cells of at most WG boxes, 32/WG cells per warp, lane r of a group holds
-// box r and tests it against the next floor(n/2) boxes of the cell
-// circularly (the BALANCE=1 sweep of d_matching, pbig.cu:804-825), so every
-// unordered pair of the cell is tested exactly once.
-template <int D, int WG, bool BIP>
+// circular half sweep over the m boxes in slots [base, base+m): lane l < m
+// tests box l against boxes l+1 .. l+floor(m/2) (mod m), lanes past m/2 one
+// fewer when m is even (the BALANCE=1 sweep of d_matching, pbig.cu:804-825),
+// so each unordered pair is tested once. Bit d of the result: partner l+d.
+template <int D, bool BIP, bool NARROW>
+__device__ __forceinline__ uint32_t sweep_diag(const PairSmem& s, const Box& me, uint32_t lane, uint32_t base,
+                                               uint32_t m, uint32_t split) {
+    const uint32_t l = lane < m ? lane : 0u;
+    const uint32_t nelm = lane < m ? (lane < (m >> 1) ? (m >> 1) : ((m - 1) >> 1)) : 0u;
+    const uint32_t dmax = m >> 1;
+    uint32_t mask = 0;
+#pragma unroll 4
+    for (uint32_t d = 1; d <= dmax; d++) {
+        uint32_t pr = l + d;
+        if (pr >= m) pr -= m;
+        const Box o = slot_get(s, base + pr);
+        mask |= (hit_bit<D, BIP, NARROW>(me, o, split) & (d <= nelm ? 1u : 0u)) << d;
+    }
+    return mask;
+}
+
+// row box against the column boxes in slots [base, base+cols8), cols8 a
+// multiple of 8 (padding slots hold dummy boxes); bit j: column j
+template <int D, bool BIP, bool NARROW>
+__device__ __forceinline__ uint32_t sweep_cols(const PairSmem& s, const Box& me, uint32_t base, uint32_t cols8,
+                                               uint32_t split) {
+    uint32_t mask = 0;
+    if (cols8 == 32) {
+#pragma unroll
+        for (uint32_t j = 0; j < 32; j++) mask |= hit_bit<D, BIP, NARROW>(me, slot_get(s, base + j), split) << j;
+    } else {
+        for (uint32_t j0 = 0; j0 < cols8; j0 += 8) {
+#pragma unroll
+            for (uint32_t jj = 0; jj < 8; jj++)
+                mask |= hit_bit<D, BIP, NARROW>(me, slot_get(s, base + j0 + jj), split) << (j0 + jj);
+        }
+    }
+    return mask;
+}
+
+// cells of at most WG boxes, 32/WG cells per warp (lane group g, box r)
+template <int D, int WG, bool BIP, bool NARROW>
 __device__ __forceinline__ void small_item(const Params& p, PairSmem& s, int list, uint64_t item,
                                            uint32_t slot0) {
     constexpr uint32_t G = 32 / WG;
@@ -491,76 +566,70 @@ __device__ __forceinline__ void small_item(const Params& p, PairSmem& s, int lis
         if (n > WG || (uint64_t)start + n > p.entry_cap) n = 0;  // inconsistent grid: skip
     }
     const bool have = r < n;
-    Box me;
-    if (have) {
-        me = load_entry<D>(p, p.entries[start + r]);
-        slot_put(s, slot0 + lane, me);
-    }
+    const Box me = have ? load_entry<D, NARROW>(p, p.entries[start + r]) : dummy_box<NARROW>();
+    slot_put(s, slot0 + lane, me);
     __syncwarp();
     const uint32_t nelm = have ? (r < (n >> 1) ? (n >> 1) : ((n - 1) >> 1)) : 0u;
-    uint32_t mask = 0;
     const uint32_t gb = slot0 + g * WG;
+    uint32_t mask = 0;
 #pragma unroll
     for (uint32_t d = 1; d <= WG / 2; d++) {
-        if (d <= nelm) {
-            uint32_t pr = r + d;
-            if (pr >= n) pr -= n;
-            if (hit<D, BIP>(me, slot_get(s, gb + pr), p.split)) mask |= 1u << d;
-        }
+        uint32_t pr = r + d;
+        if (pr >= n) pr -= n;
+        if (pr >= WG) pr = 0;  // idle lanes (n = 0): stay inside the group
+        mask |= (hit_bit<D, BIP, NARROW>(me, slot_get(s, gb + pr), p.split) & (d <= nelm ? 1u : 0u)) << d;
     }
-    emit<BIP>(p, s, mask, have ? me.id : 0u, [&](int d) {
-        uint32_t pr = r + (uint32_t)d;
+    auto pid = [&](uint32_t d) {
+        uint32_t pr = r + d;
         if (pr >= n) pr -= n;
         return slot_id(s, gb + pr);
-    });
+    };
+    emit2<BIP>(p, s, mask, pid, 0u, pid, me.id);
     __syncwarp();
 }
 
-// one 32x32 tile unit of a staged cell: rows = boxes [32r, 32r+32) of the
-// cell, columns = boxes [32x, 32x+32); x == r is the diagonal tile (circular
-// sweep), x > r a full rectangle with the column box broadcast to all lanes.
-template <int D, bool BIP>
-__device__ __forceinline__ void tile_unit(const Params& p, PairSmem& s, uint32_t row_slot0, uint32_t col_slot0,
-                                          uint32_t rows, uint32_t cols, bool diag) {
+// row tile r of a cell staged at slots [off, off + n8): the diagonal tile and
+// every column tile x > r, emitted two tiles at a time
+template <int D, bool BIP, bool NARROW>
+__device__ __forceinline__ void row_unit(const Params& p, PairSmem& s, uint32_t off, uint32_t n, uint32_t r) {
     const uint32_t lane = lane_id();
-    const bool have = lane < rows;
-    Box me;
-    if (have) me = slot_get(s, row_slot0 + lane);
-    uint32_t mask = 0;
-    if (diag) {
-        const uint32_t nelm = have ? (lane < (rows >> 1) ? (rows >> 1) : ((rows - 1) >> 1)) : 0u;
-#pragma unroll
-        for (uint32_t d = 1; d <= 16; d++) {
-            if (d <= nelm) {
-                uint32_t pr = lane + d;
-                if (pr >= rows) pr -= rows;
-                if (hit<D, BIP>(me, slot_get(s, row_slot0 + pr), p.split)) mask |= 1u << d;
-            }
+    const uint32_t R = (n + 31) >> 5;
+    const uint32_t rows = min(32u, n - 32 * r);
+    const uint32_t rbase = off + 32 * r;
+    const Box me = lane < rows ? slot_get(s, rbase + lane) : dummy_box<NARROW>();
+    const uint32_t md = sweep_diag<D, BIP, NARROW>(s, me, lane, rbase, rows, p.split);
+    auto pdiag = [&](uint32_t d) {
+        uint32_t pr = lane + d;
+        if (pr >= rows) pr -= rows;
+        return slot_id(s, rbase + pr);
+    };
+    uint32_t x = r + 1;
+    if (x >= R) {
+        emit2<BIP>(p, s, md, pdiag, 0u, pdiag, me.id);
+        return;
+    }
+    {
+        const uint32_t cb = off + 32 * x, c8 = (min(32u, n - 32 * x) + 7) & ~7u;
+        const uint32_t mc = sweep_cols<D, BIP, NARROW>(s, me, cb, c8, p.split);
+        emit2<BIP>(p, s, md, pdiag, mc, [&](uint32_t j) { return slot_id(s, cb + j); }, me.id);
+    }
+    for (x = r + 2; x < R; x += 2) {
+        const uint32_t cb1 = off + 32 * x, c81 = (min(32u, n - 32 * x) + 7) & ~7u;
+        const uint32_t m1 = sweep_cols<D, BIP, NARROW>(s, me, cb1, c81, p.split);
+        uint32_t m2 = 0, cb2 = cb1;
+        if (x + 1 < R) {
+            cb2 = off + 32 * (x + 1);
+            m2 = sweep_cols<D, BIP, NARROW>(s, me, cb2, (min(32u, n - 32 * (x + 1)) + 7) & ~7u, p.split);
         }
-        emit<BIP>(p, s, mask, have ? me.id : 0u, [&](int d) {
-            uint32_t pr = lane + (uint32_t)d;
-            if (pr >= rows) pr -= rows;
-            return slot_id(s, row_slot0 + pr);
-        });
-    } else {
-        if (have) {
-            if (cols == 32) {
-#pragma unroll
-                for (uint32_t j = 0; j < 32; j++)
-                    if (hit<D, BIP>(me, slot_get(s, col_slot0 + j), p.split)) mask |= 1u << j;
-            } else {
-                for (uint32_t j = 0; j < cols; j++)
-                    if (hit<D, BIP>(me, slot_get(s, col_slot0 + j), p.split)) mask |= 1u << j;
-            }
-        }
-        emit<BIP>(p, s, mask, have ? me.id : 0u, [&](int j) { return slot_id(s, col_slot0 + (uint32_t)j); });
+        emit2<BIP>(p, s, m1, [&](uint32_t j) { return slot_id(s, cb1 + j); }, m2,
+                   [&](uint32_t j) { return slot_id(s, cb2 + j); }, me.id);
     }
 }
 
 // cells of 33..kBigMax boxes: up to kBigCellsPerTask cells are staged whole
-// into shared memory (as many as fit), then the block's warps share their
-// 32x32 tile units.
-template <int D, bool BIP>
+// (each padded to a multiple of 8 slots), then the block's warps share their
+// row tiles.
+template <int D, bool BIP, bool NARROW>
 __device__ void big_task(const Params& p, PairSmem& s, uint64_t task) {
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const uint64_t nl = mn64(p.ctr->n_list[kListBig], p.list_cap[kListBig]);
@@ -569,32 +638,30 @@ __device__ void big_task(const Params& p, PairSmem& s, uint64_t task) {
     while (cur < end) {
         if (warp == 0) {
             uint32_t n = 0, st = 0;
-            const bool v = lane < kBigCellsPerTask && cur + lane < end;
+            const bool v = cur + lane < end;
             if (v) {
                 const uint32_t cell = p.lists[p.list_off[kListBig] + cur + lane];
                 st = p.starts[cell];
                 n = p.starts[cell + 1] - st;
                 if (n > kBigMax || (uint64_t)st + n > p.entry_cap) n = 0;  // inconsistent grid: skip
             }
-            const uint32_t inc = warp_incl_scan(n);
+            const uint32_t n8 = (n + 7) & ~7u;
+            const uint32_t inc = warp_incl_scan(n8);
             const uint32_t fits = __ballot_sync(FULL_MASK, v && inc <= kSlots);
-            const uint32_t k = __popc(fits);  // prefix property: fits is a low-bit run
-            const uint32_t R = (n + 31) >> 5;
-            const uint32_t u = (v && lane < k) ? R * (R + 1) / 2 : 0u;
-            const uint32_t uinc = warp_incl_scan(u);
+            const uint32_t k = __popc(fits);  // fits is a run of low bits
+            const uint32_t units = lane < k ? (n + 31) >> 5 : 0u;
+            const uint32_t uinc = warp_incl_scan(units);
             if (lane < k) {
                 s.cell_start[lane] = st;
                 s.cell_n[lane] = n;
-                s.cell_off[lane] = inc - n;
+                s.cell_off[lane] = inc - n8;
                 s.unit_pref[lane + 1] = uinc;
             }
-            if (lane == 0) s.unit_pref[0] = 0;
-            if (lane == 0 && k == 0) {
-                s.k = 0;
-                s.tot = 0;
-                s.units = 0;
+            if (lane == 0) {
+                s.unit_pref[0] = 0;
+                if (k == 0) s.k = s.tot = s.units = 0;
             }
-            if (lane == k - 1) {
+            if (k > 0 && lane == k - 1) {
                 s.cell_off[k] = inc;
                 s.k = k;
                 s.tot = inc;
@@ -605,20 +672,21 @@ __device__ void big_task(const Params& p, PairSmem& s, uint64_t task) {
         const uint32_t K = s.k, tot = s.tot, U = s.units;
         if (K == 0) break;  // uniform: every thread read the same K
         for (uint32_t e = t; e < tot; e += kPairThreads) {
-            uint32_t c = 0;
-            while (c + 1 < K && s.cell_off[c + 1] <= e) c++;
-            slot_put(s, e, load_entry<D>(p, p.entries[s.cell_start[c] + (e - s.cell_off[c])]));
+            uint32_t c = 0;  // last cell whose slots start at or before e
+#pragma unroll
+            for (uint32_t step = 16; step; step >>= 1)
+                if (c + step < K && s.cell_off[c + step] <= e) c += step;
+            const uint32_t local = e - s.cell_off[c];
+            slot_put(s, e, local < s.cell_n[c] ? load_entry<D, NARROW>(p, p.entries[s.cell_start[c] + local])
+                                               : dummy_box<NARROW>());
         }
         __syncthreads();
         for (uint32_t u = warp; u < U; u += kPairWarps) {
             uint32_t c = 0;
-            while (c + 1 < K && s.unit_pref[c + 1] <= u) c++;
-            uint32_t lu = u - s.unit_pref[c];
-            const uint32_t n = s.cell_n[c], off = s.cell_off[c], R = (n + 31) >> 5;
-            uint32_t r = 0;
-            while (lu >= R - r) { lu -= R - r; r++; }
-            const uint32_t x = r + lu;
-            tile_unit<D, BIP>(p, s, off + 32 * r, off + 32 * x, min(32u, n - 32 * r), min(32u, n - 32 * x), x == r);
+#pragma unroll
+            for (uint32_t step = 16; step; step >>= 1)
+                if (c + step < K && s.unit_pref[c + step] <= u) c += step;
+            row_unit<D, BIP, NARROW>(p, s, s.cell_off[c], s.cell_n[c], u - s.unit_pref[c]);
         }
         __syncthreads();
         cur += K;
@@ -626,7 +694,8 @@ __device__ void big_task(const Params& p, PairSmem& s, uint64_t task) {
 }
 
 // cells larger than kBigMax: one tile task per warp, boxes gathered per tile
-template <int D, bool BIP>
+// into the warp's 64 slots (32 rows, 32 columns)
+template <int D, bool BIP, bool NARROW>
 __device__ __forceinline__ void huge_item(const Params& p, PairSmem& s, uint64_t item, uint32_t slot0) {
     const uint32_t lane = lane_id();
     const uint64_t nt = mn64(p.ctr->need_tasks, p.task_cap);
@@ -634,23 +703,35 @@ __device__ __forceinline__ void huge_item(const Params& p, PairSmem& s, uint64_t
     const uint4 tk = p.tasks[item];
     const uint32_t cell = tk.x, r = tk.y, x0 = tk.z, x1 = tk.w;
     const uint32_t start = p.starts[cell], n = p.starts[cell + 1] - start;
-    if ((uint64_t)start + n > p.entry_cap || 32ull * r >= n || 32ull * (x1 - 1) >= n) return;
+    if ((uint64_t)start + n > p.entry_cap || 32ull * r >= n || x1 <= x0 || 32ull * (x1 - 1) >= n) return;
     const uint32_t rows = min(32u, n - 32 * r);
-    if (lane < rows) slot_put(s, slot0 + lane, load_entry<D>(p, p.entries[start + 32 * r + lane]));
+    const Box me = lane < rows ? load_entry<D, NARROW>(p, p.entries[start + 32 * r + lane]) : dummy_box<NARROW>();
+    slot_put(s, slot0 + lane, me);
     __syncwarp();
     for (uint32_t x = x0; x < x1; x++) {
-        const uint32_t cols = min(32u, n - 32 * x);
-        if (x != r) {
-            if (lane < cols) slot_put(s, slot0 + 32 + lane, load_entry<D>(p, p.entries[start + 32 * x + lane]));
+        if (x == r) {
+            const uint32_t md = sweep_diag<D, BIP, NARROW>(s, me, lane, slot0, rows, p.split);
+            auto pd = [&](uint32_t d) {
+                uint32_t pr = lane + d;
+                if (pr >= rows) pr -= rows;
+                return slot_id(s, slot0 + pr);
+            };
+            emit2<BIP>(p, s, md, pd, 0u, pd, me.id);
+        } else {
+            const uint32_t cols = min(32u, n - 32 * x);
+            slot_put(s, slot0 + 32 + lane,
+                     lane < cols ? load_entry<D, NARROW>(p, p.entries[start + 32 * x + lane]) : dummy_box<NARROW>());
             __syncwarp();
+            const uint32_t mc = sweep_cols<D, BIP, NARROW>(s, me, slot0 + 32, (cols + 7) & ~7u, p.split);
+            auto pc = [&](uint32_t j) { return slot_id(s, slot0 + 32 + j); };
+            emit2<BIP>(p, s, mc, pc, 0u, pc, me.id);
         }
-        tile_unit<D, BIP>(p, s, slot0, slot0 + 32, rows, cols, x == r);
         __syncwarp();
     }
 }
 
-template <int D, bool BIP>
-__global__ void __launch_bounds__(kPairThreads, 4) k_pairs(Params p) {
+template <int D, bool BIP, bool NARROW>
+__global__ void __launch_bounds__(kPairThreads, 3) k_pairs(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PairSmem& s = *reinterpret_cast<PairSmem*>(smem_raw);
     const uint32_t t = threadIdx.x, warp = t >> 5;
@@ -684,12 +765,12 @@ __global__ void __launch_bounds__(kPairThreads, 4) k_pairs(Params p) {
         int cls = 0;
         while (cls < kNumLists - 1 && rem >= s.nbt[cls]) { rem -= s.nbt[cls]; cls++; }
         switch (cls) {
-            case 0: small_item<D, 4, BIP>(p, s, 0, rem * kPairWarps + warp, slot0); break;
-            case 1: small_item<D, 8, BIP>(p, s, 1, rem * kPairWarps + warp, slot0); break;
-            case 2: small_item<D, 16, BIP>(p, s, 2, rem * kPairWarps + warp, slot0); break;
-            case 3: small_item<D, 32, BIP>(p, s, 3, rem * kPairWarps + warp, slot0); break;
-            case kListBig: big_task<D, BIP>(p, s, rem); break;
-            default: huge_item<D, BIP>(p, s, rem * kPairWarps + warp, slot0); break;
+            case 0: small_item<D, 4, BIP, NARROW>(p, s, 0, rem * kPairWarps + warp, slot0); break;
+            case 1: small_item<D, 8, BIP, NARROW>(p, s, 1, rem * kPairWarps + warp, slot0); break;
+            case 2: small_item<D, 16, BIP, NARROW>(p, s, 2, rem * kPairWarps + warp, slot0); break;
+            case 3: small_item<D, 32, BIP, NARROW>(p, s, 3, rem * kPairWarps + warp, slot0); break;
+            case kListBig: big_task<D, BIP, NARROW>(p, s, rem); break;
+            default: huge_item<D, BIP, NARROW>(p, s, rem * kPairWarps + warp, slot0); break;
         }
         __syncthreads();
         const uint32_t on = s.out_n, ovf = s.first_ovf;
@@ -751,13 +832,17 @@ cudaError_t kernels_init() {
 #define SET_SMEM(K)                                                                             \
     e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);               \
     if (e != cudaSuccess) return e;
-    SET_SMEM((k_pairs<2, false>));
-    SET_SMEM((k_pairs<3, false>));
-    SET_SMEM((k_pairs<2, true>));
-    SET_SMEM((k_pairs<3, true>));
+    SET_SMEM((k_pairs<2, false, true>));
+    SET_SMEM((k_pairs<3, false, true>));
+    SET_SMEM((k_pairs<2, true, true>));
+    SET_SMEM((k_pairs<3, true, true>));
+    SET_SMEM((k_pairs<2, false, false>));
+    SET_SMEM((k_pairs<3, false, false>));
+    SET_SMEM((k_pairs<2, true, false>));
+    SET_SMEM((k_pairs<3, true, false>));
 #undef SET_SMEM
     int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs<3, false>, kPairThreads, sm);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs<3, false, true>, kPairThreads, sm);
     if (e != cudaSuccess) return e;
     g_pair_blocks_per_sm = nb > 0 ? nb : 1;
     return cudaSuccess;
@@ -805,13 +890,16 @@ cudaError_t launch_expand(const Params& p, cudaStream_t st) {
 cudaError_t launch_pairs(const Params& p, int dims, int grid_blocks, cudaStream_t st) {
     const size_t sm = sizeof(PairSmem);
     const bool bip = p.split != kNoSplit;
-    if (dims == 2) {
-        if (bip) k_pairs<2, true><<<grid_blocks, kPairThreads, sm, st>>>(p);
-        else k_pairs<2, false><<<grid_blocks, kPairThreads, sm, st>>>(p);
+    const bool narrow = p.max_range <= (1u << kMissShift);
+#define LAUNCH(D, B, N) k_pairs<D, B, N><<<grid_blocks, kPairThreads, sm, st>>>(p)
+    if (narrow) {
+        if (dims == 2) { if (bip) LAUNCH(2, true, true); else LAUNCH(2, false, true); }
+        else { if (bip) LAUNCH(3, true, true); else LAUNCH(3, false, true); }
     } else {
-        if (bip) k_pairs<3, true><<<grid_blocks, kPairThreads, sm, st>>>(p);
-        else k_pairs<3, false><<<grid_blocks, kPairThreads, sm, st>>>(p);
+        if (dims == 2) { if (bip) LAUNCH(2, true, false); else LAUNCH(2, false, false); }
+        else { if (bip) LAUNCH(3, true, false); else LAUNCH(3, false, false); }
     }
+#undef LAUNCH
     return cudaGetLastError();
 }
 

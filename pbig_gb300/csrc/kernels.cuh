@@ -60,6 +60,7 @@ struct Params {
     const uint32_t* scene_box_off;// nscenes+1 box offsets (device)
     uint32_t nscenes;
     uint32_t split;               // bipartite: global index of the first blue box
+    uint32_t max_range;           // largest scene range (selects the pair-test arithmetic)
     uint32_t* counts;             // [ncells] (zero before count; zero after scatter)
     uint32_t* starts;             // [ncells+1] exclusive scan of counts
     uint64_t ncells;

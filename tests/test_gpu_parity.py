@@ -187,3 +187,19 @@ def test_harness_golden_count_on_gpu(engine):
     (test1, N = 10 M, UU, side < 100, range 10 000), through the engine."""
     boxes = O.harness_boxes(10_000_000, S=100, range_=10000, sim="UU")
     assert engine.self_intersect(to_device(boxes), 10000) == 49_514_252
+
+
+@pytest.mark.parametrize("name", ["rand3d_mixed_50000", "rand2d_4097", "identical700"])
+def test_wide_coordinates(engine, name):
+    """Ranges above 2^29 take the comparison form of the pair test: scaling
+    every coordinate by a power of two keeps the pair set."""
+    z = np.load(os.path.join(HERE, "golden", name + ".npz"))
+    boxes, rng, want = z["boxes"].astype(np.uint64), int(z["range"]), z["pairs"]
+    k = max(0, 32 - int(rng - 1).bit_length() - 1)
+    wide = boxes.copy()
+    wide[:, :-1] <<= k
+    wide = wide.astype(np.uint32)
+    rng_w = min((rng << k), 0xFFFFFFFF)
+    assert rng_w > (1 << 29)
+    assert engine.self_intersect(wide, rng_w) == len(want)
+    assert np.array_equal(canon(engine.pairs()), want)
