@@ -290,7 +290,6 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     p.ncells = ncells;
     p.tile_state = c->d_state.as<unsigned long long>();
     p.ctr = c->d_ctr.as<Ctr>();
-    const int grid = c->sm_count * pair_blocks_per_sm();
     Ctr h{};
     int launches = 0;
     bool need_full = true;
@@ -300,21 +299,21 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         // list regions: a cell of class c holds at least lo_c boxes, so with
         // E <= entry capacity no list can overflow
         const uint64_t ecap = c->d_entries.bytes / 4;
-        const uint64_t lo[kNumLists] = {2, 5, 9, 17, 33, kBigMax + 1};
+        const uint64_t lo[kNumLists] = {2, 5, 9, 17, 33, kMedMax + 1, kBigMax + 1};
         uint64_t loff = 0;
         for (int k = 0; k < kNumLists; k++) {
             p.list_off[k] = loff;
             p.list_cap[k] = ecap / lo[k] + 1;
             loff += p.list_cap[k];
         }
-        CK(c->d_lists.ensure(loff * 4, false, st));
+        CK(c->d_lists.ensure(loff * 8, false, st));
         CK(c->d_tasks.ensure(task_cap * 16, false, st));
         CK(c->d_out.ensure(out_cap * 8, false, st));
         p.counts = c->d_counts.as<uint32_t>();
         p.starts = c->d_starts.as<uint32_t>();
         p.entries = c->d_entries.as<uint32_t>();
         p.entry_cap = c->d_entries.bytes / 4;
-        p.lists = c->d_lists.as<uint32_t>();
+        p.lists = c->d_lists.as<uint2>();
         p.tasks = c->d_tasks.as<uint4>();
         p.task_cap = c->d_tasks.bytes / 16;
         p.out = c->d_out.as<uint2>();
@@ -339,8 +338,8 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
             CK(cudaMemsetAsync(&p.ctr->pairs, 0, sizeof(unsigned long long), st));
             CK(cudaMemsetAsync(&p.ctr->err, 0, sizeof(unsigned int), st));
         }
-        CK(launch_pairs(p, dims, grid, st));
-        launches += 1;
+        CK(launch_pairs(p, dims, c->sm_count, st));
+        launches += 3;
         CK(cudaEventRecord(c->evp[5], st));
         CK(cudaEventRecord(c->ev1, st));
         CK(cudaMemcpyAsync(c->h_ctr.p, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, st));

@@ -191,6 +191,7 @@ __device__ __forceinline__ int list_of(uint32_t n) {
     if (n <= 8) return 1;
     if (n <= 16) return 2;
     if (n <= 32) return 3;
+    if (n <= kMedMax) return kListMed;
     if (n <= kBigMax) return kListBig;
     return kListHuge;
 }
@@ -286,7 +287,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Params p) {
     __syncthreads();
     const unsigned long long base = s_prefix + warp_excl;
     // write starts and classify cells
-    uint32_t my_cls[kNumLists] = {0, 0, 0, 0, 0, 0};
+    uint32_t my_cls[kNumLists] = {0, 0, 0, 0, 0, 0, 0};
+    uint32_t st_all[16];
     unsigned long long tests = 0;
 #pragma unroll
     for (int r = 0; r < 4; r++) {
@@ -296,6 +298,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Params p) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             st[k] = (uint32_t)run;
+            st_all[4 * r + k] = st[k];
             run += v[4 * r + k];
             const int cl = list_of(v[4 * r + k]);
             if (cl >= 0) my_cls[cl]++;
@@ -336,7 +339,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Params p) {
             const int cl = list_of(v[4 * r + k]);
             if (cl >= 0) {
                 const uint64_t idx = (uint64_t)s_cls_base[cl] + atomicAdd(&s_cls[cl], 1u);
-                if (idx < p.list_cap[cl]) p.lists[p.list_off[cl] + idx] = (uint32_t)(c + k);
+                if (idx < p.list_cap[cl]) p.lists[p.list_off[cl] + idx] = make_uint2(st_all[4 * r + k], v[4 * r + k]);
             }
         }
     }
@@ -351,8 +354,8 @@ constexpr uint32_t kTaskCols = 8;
 __global__ void k_expand(Params p) {
     const uint32_t nh = mn64(p.ctr->n_list[kListHuge], p.list_cap[kListHuge]);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nh; i += gridDim.x * blockDim.x) {
-        const uint32_t cell = p.lists[p.list_off[kListHuge] + i];
-        const uint32_t n = p.starts[cell + 1] - p.starts[cell];
+        const uint2 sn = p.lists[p.list_off[kListHuge] + i];
+        const uint32_t n = sn.y;
         const uint32_t R = (n + 31) >> 5;
         uint32_t cnt = 0;
         for (uint32_t r = 0; r < R; r++) cnt += (R - r + kTaskCols - 1) / kTaskCols;
@@ -360,7 +363,7 @@ __global__ void k_expand(Params p) {
         uint32_t k = 0;
         for (uint32_t r = 0; r < R; r++)
             for (uint32_t x0 = r; x0 < R; x0 += kTaskCols, k++)
-                if ((uint64_t)b + k < p.task_cap) p.tasks[b + k] = make_uint4(cell, r, x0, min(x0 + kTaskCols, R));
+                if ((uint64_t)b + k < p.task_cap) p.tasks[b + k] = make_uint4(sn.x, n, r, x0);
         if ((uint64_t)b + cnt > p.task_cap) atomicOr(&p.ctr->err, kErrTaskOvf);
     }
 }
@@ -368,11 +371,16 @@ __global__ void k_expand(Params p) {
 // ---------------------------------------------------------------------------
 // pair test
 //
-// Work classes (block tasks, static round robin over the grid):
-//   small  cells of 2..32 boxes, 32/WG cells per warp, circular half sweep
-//   big    cells of 33..kBigMax boxes: whole cells staged in shared memory,
-//          warps take row tiles (32 boxes) and sweep all column tiles
-//   huge   cells above kBigMax: tile tasks, boxes gathered per tile
+// Three kernels share the per-pair test and the sweeps:
+//   k_pairs_small  cells of 2..32 boxes, 32/WG cells per warp item
+//   k_pairs_med    cells of 33..kMedMax boxes, one cell per warp item,
+//                  staged whole in the warp's shared memory
+//   k_pairs_block  cells of kMedMax+1..kBigMax boxes staged whole by a
+//                  block, and 32x32 tile tasks of larger cells
+// Warp items run independently (no block barriers); each warp compacts its
+// pairs into its own shared-memory buffer and flushes it to the pair array
+// with one global reservation per flush.
+//
 // The test of one (row box, column box) pair is branch free: with every
 // coordinate < 2^29 the six differences max-min are non-negative exactly
 // when the closed intervals overlap, and a negative difference sets bits
@@ -382,40 +390,36 @@ __global__ void k_expand(Params p) {
 // ---------------------------------------------------------------------------
 constexpr int kPairThreads = 256;
 constexpr int kPairWarps = kPairThreads / 32;
-constexpr uint32_t kSlots = 1024;          // staged boxes per block (32 B each)
-constexpr uint32_t kOutBuf = 4096;         // block output buffer (pairs)
-constexpr uint32_t kFlushAt = 2048;
-constexpr uint32_t kBigCellsPerTask = 32;
 constexpr uint32_t kMissShift = 29;
+constexpr uint32_t kWarpOut = 256;          // per-warp output buffer (pairs)
+constexpr uint32_t kSmallSlots = 32;        // per-warp staging, small cells
+constexpr uint32_t kMedSlots = kMedMax;     // per-warp staging, medium cells
+constexpr uint32_t kBlockSlots = kBigMax;   // per-block staging, big cells
+constexpr uint32_t kBlockOut = 2048;        // per-block output buffer (pairs)
+constexpr uint32_t kBigCellsPerTask = 8;
 
 struct Box {
     uint32_t x0, x1, y0, y1, z0, z1, f, id;  // f: axes where the box does not start in this cell, << 29
 };
 
-struct PairSmem {
-    uint4 a[kSlots];  // x0 x1 y0 y1
-    uint4 b[kSlots];  // z0 z1 f id
-    uint2 out[kOutBuf];
-    uint32_t out_n, first_ovf;
-    unsigned long long gbase;
-    uint32_t cell_start[kBigCellsPerTask], cell_n[kBigCellsPerTask], cell_off[kBigCellsPerTask + 1];
-    uint32_t unit_pref[kBigCellsPerTask + 1];
-    uint32_t k, tot, units;
-    unsigned long long nbt[kNumLists];
+// staging arrays in shared memory: slot i = (a[i], b[i])
+struct Slots {
+    uint4* a;  // x0 x1 y0 y1
+    uint4* b;  // z0 z1 f id
 };
 
-__device__ __forceinline__ void slot_put(PairSmem& s, uint32_t i, const Box& x) {
+__device__ __forceinline__ void slot_put(const Slots& s, uint32_t i, const Box& x) {
     s.a[i] = make_uint4(x.x0, x.x1, x.y0, x.y1);
     s.b[i] = make_uint4(x.z0, x.z1, x.f, x.id);
 }
-__device__ __forceinline__ Box slot_get(const PairSmem& s, uint32_t i) {
+__device__ __forceinline__ Box slot_get(const Slots& s, uint32_t i) {
     const uint4 a = s.a[i], b = s.b[i];
     Box x;
     x.x0 = a.x; x.x1 = a.y; x.y0 = a.z; x.y1 = a.w;
     x.z0 = b.x; x.z1 = b.y; x.f = b.z; x.id = b.w;
     return x;
 }
-__device__ __forceinline__ uint32_t slot_id(const PairSmem& s, uint32_t i) { return s.b[i].w; }
+__device__ __forceinline__ uint32_t slot_id(const Slots& s, uint32_t i) { return s.b[i].w; }
 
 // a box that overlaps nothing (pads tiles to multiples of 8 and idle lanes)
 template <bool NARROW>
@@ -429,7 +433,7 @@ __device__ __forceinline__ Box dummy_box() {
 }
 
 template <int D, bool NARROW>
-__device__ __forceinline__ Box load_entry(const Params& p, uint32_t raw) {
+__device__ __forceinline__ Box load_box(const Params& p, uint32_t raw) {
     Box x;
     x.id = raw & kIdMask;
     x.f = (~(raw >> kIdBits) & 7u) << kMissShift;
@@ -461,12 +465,267 @@ __device__ __forceinline__ uint32_t hit_bit(const Box& a, const Box& b, uint32_t
     return ok;
 }
 
-// warp-wide compaction of the set bits of two masks into the block buffer
-// (ballot/popc-style ranks from one warp scan and one shared-memory
-// reservation per call); when the buffer is full the warp reserves global
-// space itself.
+// circular half sweep over the m boxes in slots [base, base+m): lane l < m
+// tests box l against boxes l+1 .. l+floor(m/2) (mod m), lanes past m/2 one
+// fewer when m is even (the BALANCE=1 sweep of d_matching, pbig.cu:804-825),
+// so each unordered pair is tested once. Bit d of the result: partner l+d.
+template <int D, bool BIP, bool NARROW>
+__device__ __forceinline__ uint32_t sweep_diag(const Slots& s, const Box& me, uint32_t lane, uint32_t base,
+                                               uint32_t m, uint32_t split) {
+    const uint32_t l = lane < m ? lane : 0u;
+    const uint32_t nelm = lane < m ? (lane < (m >> 1) ? (m >> 1) : ((m - 1) >> 1)) : 0u;
+    const uint32_t dmax = m >> 1;
+    uint32_t mask = 0;
+#pragma unroll 4
+    for (uint32_t d = 1; d <= dmax; d++) {
+        uint32_t pr = l + d;
+        if (pr >= m) pr -= m;
+        mask |= (hit_bit<D, BIP, NARROW>(me, slot_get(s, base + pr), split) & (d <= nelm ? 1u : 0u)) << d;
+    }
+    return mask;
+}
+
+// row box against the column boxes in slots [base, base+cols8), cols8 a
+// multiple of 8 (padding slots hold dummy boxes); bit j: column j
+template <int D, bool BIP, bool NARROW>
+__device__ __forceinline__ uint32_t sweep_cols(const Slots& s, const Box& me, uint32_t base, uint32_t cols8,
+                                               uint32_t split) {
+    uint32_t mask = 0;
+    if (cols8 == 32) {
+#pragma unroll
+        for (uint32_t j = 0; j < 32; j++) mask |= hit_bit<D, BIP, NARROW>(me, slot_get(s, base + j), split) << j;
+    } else {
+        for (uint32_t j0 = 0; j0 < cols8; j0 += 8) {
+#pragma unroll
+            for (uint32_t jj = 0; jj < 8; jj++)
+                mask |= hit_bit<D, BIP, NARROW>(me, slot_get(s, base + j0 + jj), split) << (j0 + jj);
+        }
+    }
+    return mask;
+}
+
+// ---- output: warp-private buffer ------------------------------------------
+struct WarpOut {
+    uint2* buf;
+    uint32_t n;  // warp-uniform fill
+};
+
+__device__ __forceinline__ void wflush(const Params& p, WarpOut& o) {
+    if (o.n == 0) return;
+    const uint32_t lane = lane_id();
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&p.ctr->pairs, (unsigned long long)o.n);
+    base = __shfl_sync(FULL_MASK, base, 0);
+    __syncwarp();
+    for (uint32_t k = lane; k < o.n; k += 32) {
+        const unsigned long long g = base + k;
+        if (g < p.out_cap) p.out[g] = o.buf[k];
+        else atomicOr(&p.ctr->err, kErrOutOvf);
+    }
+    __syncwarp();
+    o.n = 0;
+}
+
+// compaction of the set bits of two masks (ranks from one warp scan of the
+// per-lane popcounts) into the warp buffer, or straight to the pair array
+// when the batch is larger than the buffer
 template <bool BIP, class PA, class PB>
-__device__ __forceinline__ void emit2(const Params& p, PairSmem& s, uint32_t ma, PA pa, uint32_t mb, PB pb,
+__device__ __forceinline__ void wemit(const Params& p, WarpOut& o, uint32_t ma, PA pa, uint32_t mb, PB pb,
+                                      uint32_t myid) {
+    const uint32_t lane = lane_id();
+    const uint32_t k = __popc(ma) + __popc(mb);
+    const uint32_t incl = warp_incl_scan(k);
+    const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+    if (total == 0) return;
+    bool direct = false;
+    unsigned long long gbase = 0;
+    if (o.n + total > kWarpOut) {
+        wflush(p, o);
+        if (total > kWarpOut) {
+            direct = true;
+            if (lane == 0) gbase = atomicAdd(&p.ctr->pairs, (unsigned long long)total);
+            gbase = __shfl_sync(FULL_MASK, gbase, 0);
+        }
+    }
+    uint32_t w = incl - k;
+    auto put = [&](uint32_t q) {
+        uint2 pr = make_uint2(min(myid, q), max(myid, q));
+        if (BIP) pr.y -= p.split;
+        if (!direct) {
+            o.buf[o.n + w] = pr;
+        } else {
+            const unsigned long long g = gbase + w;
+            if (g < p.out_cap) p.out[g] = pr;
+            else atomicOr(&p.ctr->err, kErrOutOvf);
+        }
+        w++;
+    };
+    while (ma) {
+        const uint32_t bit = __ffs(ma) - 1;
+        ma &= ma - 1;
+        put(pa(bit));
+    }
+    while (mb) {
+        const uint32_t bit = __ffs(mb) - 1;
+        mb &= mb - 1;
+        put(pb(bit));
+    }
+    __syncwarp();
+    if (!direct) o.n += total;
+}
+
+// row tile r of a cell staged at slots [off, off + n8): the diagonal tile and
+// every column tile x > r, emitted two tiles at a time
+template <int D, bool BIP, bool NARROW, class Emit>
+__device__ __forceinline__ void row_unit(const Params& p, const Slots& s, uint32_t off, uint32_t n, uint32_t r,
+                                         Emit emit) {
+    const uint32_t lane = lane_id();
+    const uint32_t R = (n + 31) >> 5;
+    const uint32_t rows = min(32u, n - 32 * r);
+    const uint32_t rbase = off + 32 * r;
+    const Box me = lane < rows ? slot_get(s, rbase + lane) : dummy_box<NARROW>();
+    const uint32_t md = sweep_diag<D, BIP, NARROW>(s, me, lane, rbase, rows, p.split);
+    auto pdiag = [&](uint32_t d) {
+        uint32_t pr = lane + d;
+        if (pr >= rows) pr -= rows;
+        return slot_id(s, rbase + pr);
+    };
+    uint32_t x = r + 1;
+    if (x >= R) {
+        emit(md, pdiag, 0u, pdiag, me.id);
+        return;
+    }
+    {
+        const uint32_t cb = off + 32 * x, c8 = (min(32u, n - 32 * x) + 7) & ~7u;
+        const uint32_t mc = sweep_cols<D, BIP, NARROW>(s, me, cb, c8, p.split);
+        emit(md, pdiag, mc, [&](uint32_t j) { return slot_id(s, cb + j); }, me.id);
+    }
+    for (x = r + 2; x < R; x += 2) {
+        const uint32_t cb1 = off + 32 * x, c81 = (min(32u, n - 32 * x) + 7) & ~7u;
+        const uint32_t m1 = sweep_cols<D, BIP, NARROW>(s, me, cb1, c81, p.split);
+        uint32_t m2 = 0, cb2 = cb1;
+        if (x + 1 < R) {
+            cb2 = off + 32 * (x + 1);
+            m2 = sweep_cols<D, BIP, NARROW>(s, me, cb2, (min(32u, n - 32 * (x + 1)) + 7) & ~7u, p.split);
+        }
+        emit(m1, [&](uint32_t j) { return slot_id(s, cb1 + j); }, m2, [&](uint32_t j) { return slot_id(s, cb2 + j); },
+             me.id);
+    }
+}
+
+// ---- small cells ------------------------------------------------------------
+// lane group g (WG lanes) holds cell item*G+g of the class list, lane r its
+// box r; the circular half sweep runs inside the group.
+template <int D, int WG, bool BIP, bool NARROW>
+__device__ __forceinline__ void small_items(const Params& p, const Slots& s, WarpOut& o, int list, uint64_t first,
+                                            uint64_t stride) {
+    constexpr uint32_t G = 32 / WG;
+    const uint32_t lane = lane_id(), g = lane / WG, r = lane % WG;
+    const uint64_t nl = mn64(p.ctr->n_list[list], p.list_cap[list]);
+    const uint64_t nitems = (nl + G - 1) / G;
+    const uint32_t gb = g * WG;
+    for (uint64_t item = first; item < nitems; item += stride) {
+        const uint64_t ci = item * G + g;
+        uint32_t n = 0, start = 0;
+        if (ci < nl) {
+            const uint2 sn = p.lists[p.list_off[list] + ci];
+            start = sn.x;
+            n = sn.y;
+            if (n > WG || (uint64_t)start + n > p.entry_cap) n = 0;  // inconsistent grid: skip
+        }
+        const bool have = r < n;
+        const Box me = have ? load_box<D, NARROW>(p, p.entries[start + r]) : dummy_box<NARROW>();
+        slot_put(s, lane, me);
+        __syncwarp();
+        const uint32_t nelm = have ? (r < (n >> 1) ? (n >> 1) : ((n - 1) >> 1)) : 0u;
+        uint32_t mask = 0;
+#pragma unroll
+        for (uint32_t d = 1; d <= WG / 2; d++) {
+            uint32_t pr = r + d;
+            if (pr >= n) pr -= n;
+            if (pr >= WG) pr = 0;  // idle lanes (n = 0) stay inside the group
+            mask |= (hit_bit<D, BIP, NARROW>(me, slot_get(s, gb + pr), p.split) & (d <= nelm ? 1u : 0u)) << d;
+        }
+        auto pid = [&](uint32_t d) {
+            uint32_t pr = r + d;
+            if (pr >= n) pr -= n;
+            return slot_id(s, gb + pr);
+        };
+        wemit<BIP>(p, o, mask, pid, 0u, pid, me.id);
+    }
+}
+
+template <int D, bool BIP, bool NARROW>
+__global__ void __launch_bounds__(kPairThreads, 6) k_pairs_small(Params p) {
+    __shared__ uint4 s_a[kPairWarps][kSmallSlots], s_b[kPairWarps][kSmallSlots];
+    __shared__ uint2 s_out[kPairWarps][kWarpOut];
+    const uint32_t warp = threadIdx.x >> 5;
+    const Slots s{s_a[warp], s_b[warp]};
+    WarpOut o{s_out[warp], 0};
+    const uint64_t gw = (uint64_t)blockIdx.x * kPairWarps + warp, nw = (uint64_t)gridDim.x * kPairWarps;
+    // classes interleaved over the warps so every warp gets a similar mix
+    small_items<D, 32, BIP, NARROW>(p, s, o, 3, gw, nw);
+    small_items<D, 16, BIP, NARROW>(p, s, o, 2, (gw + nw / 4) % nw, nw);
+    small_items<D, 8, BIP, NARROW>(p, s, o, 1, (gw + nw / 2) % nw, nw);
+    small_items<D, 4, BIP, NARROW>(p, s, o, 0, (gw + 3 * nw / 4) % nw, nw);
+    wflush(p, o);
+}
+
+// ---- medium cells: one per warp item, staged whole ---------------------------
+template <int D, bool BIP, bool NARROW>
+__global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    uint4* base = reinterpret_cast<uint4*>(smem_raw);
+    const Slots s{base + warp * 2 * kMedSlots, base + warp * 2 * kMedSlots + kMedSlots};
+    uint2* obuf = reinterpret_cast<uint2*>(base + kPairWarps * 2 * kMedSlots) + warp * kWarpOut;
+    WarpOut o{obuf, 0};
+    const uint64_t nl = mn64(p.ctr->n_list[kListMed], p.list_cap[kListMed]);
+    const uint64_t nw = (uint64_t)gridDim.x * kPairWarps;
+    auto emit = [&](uint32_t ma, auto pa, uint32_t mb, auto pb, uint32_t myid) { wemit<BIP>(p, o, ma, pa, mb, pb, myid); };
+    for (uint64_t item = (uint64_t)blockIdx.x * kPairWarps + warp; item < nl; item += nw) {
+        const uint2 sn = p.lists[p.list_off[kListMed] + item];
+        const uint32_t start = sn.x;
+        uint32_t n = sn.y;
+        if (n > kMedMax || (uint64_t)start + n > p.entry_cap) continue;  // inconsistent grid: skip
+        const uint32_t n8 = (n + 7) & ~7u;
+        // stage: all entry ids first, then all boxes (loads in flight together)
+        uint32_t raw[kMedSlots / 32];
+#pragma unroll
+        for (uint32_t k = 0; k < kMedSlots / 32; k++) {
+            const uint32_t e = lane + 32 * k;
+            raw[k] = e < n ? p.entries[start + e] : 0u;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kMedSlots / 32; k++) {
+            const uint32_t e = lane + 32 * k;
+            if (e < n8) slot_put(s, e, e < n ? load_box<D, NARROW>(p, raw[k]) : dummy_box<NARROW>());
+        }
+        __syncwarp();
+        const uint32_t R = (n + 31) >> 5;
+        for (uint32_t r = 0; r < R; r++) row_unit<D, BIP, NARROW>(p, s, 0, n, r, emit);
+        __syncwarp();
+    }
+    wflush(p, o);
+}
+
+// ---- big cells (block staged) and huge cells (tiles) -----------------------
+struct BlockSmem {
+    uint4 a[kBlockSlots];
+    uint4 b[kBlockSlots];
+    uint2 out[kBlockOut];
+    uint32_t out_n, first_ovf;
+    unsigned long long gbase;
+    uint32_t cell_start[kBigCellsPerTask], cell_n[kBigCellsPerTask], cell_off[kBigCellsPerTask + 1];
+    uint32_t unit_pref[kBigCellsPerTask + 1];
+    uint32_t k, tot, units;
+    unsigned long long nbt[2];
+};
+
+// block-buffer compaction (shared reservation per warp call); when the
+// buffer is full the warp reserves global space itself
+template <bool BIP, class PA, class PB>
+__device__ __forceinline__ void bemit(const Params& p, BlockSmem& s, uint32_t ma, PA pa, uint32_t mb, PB pb,
                                       uint32_t myid) {
     const uint32_t lane = lane_id();
     const uint32_t k = __popc(ma) + __popc(mb);
@@ -477,14 +736,14 @@ __device__ __forceinline__ void emit2(const Params& p, PairSmem& s, uint32_t ma,
     unsigned long long gbase = 0;
     if (lane == 0) {
         pos = atomicAdd(&s.out_n, total);
-        if (pos + total > kOutBuf) {
+        if (pos + total > kBlockOut) {
             atomicMin(&s.first_ovf, pos);
             gbase = atomicAdd(&p.ctr->pairs, (unsigned long long)total);
         }
     }
     pos = __shfl_sync(FULL_MASK, pos, 0);
     gbase = __shfl_sync(FULL_MASK, gbase, 0);
-    const bool direct = pos + total > kOutBuf;
+    const bool direct = pos + total > kBlockOut;
     uint32_t w = incl - k;
     auto put = [&](uint32_t q) {
         uint2 pr = make_uint2(min(myid, q), max(myid, q));
@@ -510,144 +769,27 @@ __device__ __forceinline__ void emit2(const Params& p, PairSmem& s, uint32_t ma,
     }
 }
 
-// circular half sweep over the m boxes in slots [base, base+m): lane l < m
-// tests box l against boxes l+1 .. l+floor(m/2) (mod m), lanes past m/2 one
-// fewer when m is even (the BALANCE=1 sweep of d_matching, pbig.cu:804-825),
-// so each unordered pair is tested once. Bit d of the result: partner l+d.
 template <int D, bool BIP, bool NARROW>
-__device__ __forceinline__ uint32_t sweep_diag(const PairSmem& s, const Box& me, uint32_t lane, uint32_t base,
-                                               uint32_t m, uint32_t split) {
-    const uint32_t l = lane < m ? lane : 0u;
-    const uint32_t nelm = lane < m ? (lane < (m >> 1) ? (m >> 1) : ((m - 1) >> 1)) : 0u;
-    const uint32_t dmax = m >> 1;
-    uint32_t mask = 0;
-#pragma unroll 4
-    for (uint32_t d = 1; d <= dmax; d++) {
-        uint32_t pr = l + d;
-        if (pr >= m) pr -= m;
-        const Box o = slot_get(s, base + pr);
-        mask |= (hit_bit<D, BIP, NARROW>(me, o, split) & (d <= nelm ? 1u : 0u)) << d;
-    }
-    return mask;
-}
-
-// row box against the column boxes in slots [base, base+cols8), cols8 a
-// multiple of 8 (padding slots hold dummy boxes); bit j: column j
-template <int D, bool BIP, bool NARROW>
-__device__ __forceinline__ uint32_t sweep_cols(const PairSmem& s, const Box& me, uint32_t base, uint32_t cols8,
-                                               uint32_t split) {
-    uint32_t mask = 0;
-    if (cols8 == 32) {
-#pragma unroll
-        for (uint32_t j = 0; j < 32; j++) mask |= hit_bit<D, BIP, NARROW>(me, slot_get(s, base + j), split) << j;
-    } else {
-        for (uint32_t j0 = 0; j0 < cols8; j0 += 8) {
-#pragma unroll
-            for (uint32_t jj = 0; jj < 8; jj++)
-                mask |= hit_bit<D, BIP, NARROW>(me, slot_get(s, base + j0 + jj), split) << (j0 + jj);
-        }
-    }
-    return mask;
-}
-
-// cells of at most WG boxes, 32/WG cells per warp (lane group g, box r)
-template <int D, int WG, bool BIP, bool NARROW>
-__device__ __forceinline__ void small_item(const Params& p, PairSmem& s, int list, uint64_t item,
-                                           uint32_t slot0) {
-    constexpr uint32_t G = 32 / WG;
-    const uint32_t lane = lane_id(), g = lane / WG, r = lane % WG;
-    const uint64_t ci = item * G + g;
-    const uint64_t nl = mn64(p.ctr->n_list[list], p.list_cap[list]);
-    uint32_t n = 0, start = 0;
-    if (ci < nl) {
-        const uint32_t cell = p.lists[p.list_off[list] + ci];
-        start = p.starts[cell];
-        n = p.starts[cell + 1] - start;
-        if (n > WG || (uint64_t)start + n > p.entry_cap) n = 0;  // inconsistent grid: skip
-    }
-    const bool have = r < n;
-    const Box me = have ? load_entry<D, NARROW>(p, p.entries[start + r]) : dummy_box<NARROW>();
-    slot_put(s, slot0 + lane, me);
-    __syncwarp();
-    const uint32_t nelm = have ? (r < (n >> 1) ? (n >> 1) : ((n - 1) >> 1)) : 0u;
-    const uint32_t gb = slot0 + g * WG;
-    uint32_t mask = 0;
-#pragma unroll
-    for (uint32_t d = 1; d <= WG / 2; d++) {
-        uint32_t pr = r + d;
-        if (pr >= n) pr -= n;
-        if (pr >= WG) pr = 0;  // idle lanes (n = 0): stay inside the group
-        mask |= (hit_bit<D, BIP, NARROW>(me, slot_get(s, gb + pr), p.split) & (d <= nelm ? 1u : 0u)) << d;
-    }
-    auto pid = [&](uint32_t d) {
-        uint32_t pr = r + d;
-        if (pr >= n) pr -= n;
-        return slot_id(s, gb + pr);
-    };
-    emit2<BIP>(p, s, mask, pid, 0u, pid, me.id);
-    __syncwarp();
-}
-
-// row tile r of a cell staged at slots [off, off + n8): the diagonal tile and
-// every column tile x > r, emitted two tiles at a time
-template <int D, bool BIP, bool NARROW>
-__device__ __forceinline__ void row_unit(const Params& p, PairSmem& s, uint32_t off, uint32_t n, uint32_t r) {
-    const uint32_t lane = lane_id();
-    const uint32_t R = (n + 31) >> 5;
-    const uint32_t rows = min(32u, n - 32 * r);
-    const uint32_t rbase = off + 32 * r;
-    const Box me = lane < rows ? slot_get(s, rbase + lane) : dummy_box<NARROW>();
-    const uint32_t md = sweep_diag<D, BIP, NARROW>(s, me, lane, rbase, rows, p.split);
-    auto pdiag = [&](uint32_t d) {
-        uint32_t pr = lane + d;
-        if (pr >= rows) pr -= rows;
-        return slot_id(s, rbase + pr);
-    };
-    uint32_t x = r + 1;
-    if (x >= R) {
-        emit2<BIP>(p, s, md, pdiag, 0u, pdiag, me.id);
-        return;
-    }
-    {
-        const uint32_t cb = off + 32 * x, c8 = (min(32u, n - 32 * x) + 7) & ~7u;
-        const uint32_t mc = sweep_cols<D, BIP, NARROW>(s, me, cb, c8, p.split);
-        emit2<BIP>(p, s, md, pdiag, mc, [&](uint32_t j) { return slot_id(s, cb + j); }, me.id);
-    }
-    for (x = r + 2; x < R; x += 2) {
-        const uint32_t cb1 = off + 32 * x, c81 = (min(32u, n - 32 * x) + 7) & ~7u;
-        const uint32_t m1 = sweep_cols<D, BIP, NARROW>(s, me, cb1, c81, p.split);
-        uint32_t m2 = 0, cb2 = cb1;
-        if (x + 1 < R) {
-            cb2 = off + 32 * (x + 1);
-            m2 = sweep_cols<D, BIP, NARROW>(s, me, cb2, (min(32u, n - 32 * (x + 1)) + 7) & ~7u, p.split);
-        }
-        emit2<BIP>(p, s, m1, [&](uint32_t j) { return slot_id(s, cb1 + j); }, m2,
-                   [&](uint32_t j) { return slot_id(s, cb2 + j); }, me.id);
-    }
-}
-
-// cells of 33..kBigMax boxes: up to kBigCellsPerTask cells are staged whole
-// (each padded to a multiple of 8 slots), then the block's warps share their
-// row tiles.
-template <int D, bool BIP, bool NARROW>
-__device__ void big_task(const Params& p, PairSmem& s, uint64_t task) {
+__device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    const Slots sl{s.a, s.b};
+    auto emit = [&](uint32_t ma, auto pa, uint32_t mb, auto pb, uint32_t myid) { bemit<BIP>(p, s, ma, pa, mb, pb, myid); };
     const uint64_t nl = mn64(p.ctr->n_list[kListBig], p.list_cap[kListBig]);
     uint64_t cur = task * kBigCellsPerTask;
     const uint64_t end = mn64(cur + kBigCellsPerTask, nl);
     while (cur < end) {
         if (warp == 0) {
             uint32_t n = 0, st = 0;
-            const bool v = cur + lane < end;
+            const bool v = lane < kBigCellsPerTask && cur + lane < end;
             if (v) {
-                const uint32_t cell = p.lists[p.list_off[kListBig] + cur + lane];
-                st = p.starts[cell];
-                n = p.starts[cell + 1] - st;
+                const uint2 sn = p.lists[p.list_off[kListBig] + cur + lane];
+                st = sn.x;
+                n = sn.y;
                 if (n > kBigMax || (uint64_t)st + n > p.entry_cap) n = 0;  // inconsistent grid: skip
             }
             const uint32_t n8 = (n + 7) & ~7u;
             const uint32_t inc = warp_incl_scan(n8);
-            const uint32_t fits = __ballot_sync(FULL_MASK, v && inc <= kSlots);
+            const uint32_t fits = __ballot_sync(FULL_MASK, v && inc <= kBlockSlots);
             const uint32_t k = __popc(fits);  // fits is a run of low bits
             const uint32_t units = lane < k ? (n + 31) >> 5 : 0u;
             const uint32_t uinc = warp_incl_scan(units);
@@ -674,109 +816,87 @@ __device__ void big_task(const Params& p, PairSmem& s, uint64_t task) {
         for (uint32_t e = t; e < tot; e += kPairThreads) {
             uint32_t c = 0;  // last cell whose slots start at or before e
 #pragma unroll
-            for (uint32_t step = 16; step; step >>= 1)
+            for (uint32_t step = 4; step; step >>= 1)
                 if (c + step < K && s.cell_off[c + step] <= e) c += step;
             const uint32_t local = e - s.cell_off[c];
-            slot_put(s, e, local < s.cell_n[c] ? load_entry<D, NARROW>(p, p.entries[s.cell_start[c] + local])
-                                               : dummy_box<NARROW>());
+            slot_put(sl, e, local < s.cell_n[c] ? load_box<D, NARROW>(p, p.entries[s.cell_start[c] + local])
+                                                : dummy_box<NARROW>());
         }
         __syncthreads();
         for (uint32_t u = warp; u < U; u += kPairWarps) {
             uint32_t c = 0;
 #pragma unroll
-            for (uint32_t step = 16; step; step >>= 1)
+            for (uint32_t step = 4; step; step >>= 1)
                 if (c + step < K && s.unit_pref[c + step] <= u) c += step;
-            row_unit<D, BIP, NARROW>(p, s, s.cell_off[c], s.cell_n[c], u - s.unit_pref[c]);
+            row_unit<D, BIP, NARROW>(p, sl, s.cell_off[c], s.cell_n[c], u - s.unit_pref[c], emit);
         }
         __syncthreads();
         cur += K;
     }
 }
 
-// cells larger than kBigMax: one tile task per warp, boxes gathered per tile
-// into the warp's 64 slots (32 rows, 32 columns)
+// huge cells: one tile task {start, n, r, x0} per warp; boxes gathered per
+// tile into the warp's 64 slots (32 rows, 32 columns)
 template <int D, bool BIP, bool NARROW>
-__device__ __forceinline__ void huge_item(const Params& p, PairSmem& s, uint64_t item, uint32_t slot0) {
+__device__ __forceinline__ void huge_item(const Params& p, BlockSmem& s, uint64_t item, uint32_t slot0) {
     const uint32_t lane = lane_id();
+    const Slots sl{s.a, s.b};
     const uint64_t nt = mn64(p.ctr->need_tasks, p.task_cap);
     if (item >= nt) return;
     const uint4 tk = p.tasks[item];
-    const uint32_t cell = tk.x, r = tk.y, x0 = tk.z, x1 = tk.w;
-    const uint32_t start = p.starts[cell], n = p.starts[cell + 1] - start;
-    if ((uint64_t)start + n > p.entry_cap || 32ull * r >= n || x1 <= x0 || 32ull * (x1 - 1) >= n) return;
+    const uint32_t start = tk.x, n = tk.y, r = tk.z, x0 = tk.w;
+    const uint32_t R = (n + 31) >> 5;
+    const uint32_t x1 = min(x0 + kTaskCols, R);
+    if ((uint64_t)start + n > p.entry_cap || r >= R || x0 >= R) return;
     const uint32_t rows = min(32u, n - 32 * r);
-    const Box me = lane < rows ? load_entry<D, NARROW>(p, p.entries[start + 32 * r + lane]) : dummy_box<NARROW>();
-    slot_put(s, slot0 + lane, me);
+    const Box me = lane < rows ? load_box<D, NARROW>(p, p.entries[start + 32 * r + lane]) : dummy_box<NARROW>();
+    slot_put(sl, slot0 + lane, me);
     __syncwarp();
     for (uint32_t x = x0; x < x1; x++) {
         if (x == r) {
-            const uint32_t md = sweep_diag<D, BIP, NARROW>(s, me, lane, slot0, rows, p.split);
+            const uint32_t md = sweep_diag<D, BIP, NARROW>(sl, me, lane, slot0, rows, p.split);
             auto pd = [&](uint32_t d) {
                 uint32_t pr = lane + d;
                 if (pr >= rows) pr -= rows;
-                return slot_id(s, slot0 + pr);
+                return slot_id(sl, slot0 + pr);
             };
-            emit2<BIP>(p, s, md, pd, 0u, pd, me.id);
+            bemit<BIP>(p, s, md, pd, 0u, pd, me.id);
         } else {
             const uint32_t cols = min(32u, n - 32 * x);
-            slot_put(s, slot0 + 32 + lane,
-                     lane < cols ? load_entry<D, NARROW>(p, p.entries[start + 32 * x + lane]) : dummy_box<NARROW>());
+            slot_put(sl, slot0 + 32 + lane,
+                     lane < cols ? load_box<D, NARROW>(p, p.entries[start + 32 * x + lane]) : dummy_box<NARROW>());
             __syncwarp();
-            const uint32_t mc = sweep_cols<D, BIP, NARROW>(s, me, slot0 + 32, (cols + 7) & ~7u, p.split);
-            auto pc = [&](uint32_t j) { return slot_id(s, slot0 + 32 + j); };
-            emit2<BIP>(p, s, mc, pc, 0u, pc, me.id);
+            const uint32_t mc = sweep_cols<D, BIP, NARROW>(sl, me, slot0 + 32, (cols + 7) & ~7u, p.split);
+            auto pc = [&](uint32_t j) { return slot_id(sl, slot0 + 32 + j); };
+            bemit<BIP>(p, s, mc, pc, 0u, pc, me.id);
         }
         __syncwarp();
     }
 }
 
 template <int D, bool BIP, bool NARROW>
-__global__ void __launch_bounds__(kPairThreads, 3) k_pairs(Params p) {
+__global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    PairSmem& s = *reinterpret_cast<PairSmem*>(smem_raw);
+    BlockSmem& s = *reinterpret_cast<BlockSmem*>(smem_raw);
     const uint32_t t = threadIdx.x, warp = t >> 5;
     if (t == 0) {
         s.out_n = 0;
-        s.first_ovf = kOutBuf;
-    }
-    // block-task space: [small classes][big groups][huge tile tasks]
-    if (t < kNumLists) {
-        uint64_t nl;
-        uint32_t per;
-        if (t < 4) {
-            nl = mn64(p.ctr->n_list[t], p.list_cap[t]);
-            per = kPairWarps * (32u >> (2 + t));  // warps x cells per warp (WG = 4,8,16,32)
-        } else if (t == kListBig) {
-            nl = mn64(p.ctr->n_list[kListBig], p.list_cap[kListBig]);
-            per = kBigCellsPerTask;
-        } else {
-            nl = mn64(p.ctr->need_tasks, p.task_cap);
-            per = kPairWarps;
-        }
-        s.nbt[t] = (nl + per - 1) / per;
+        s.first_ovf = kBlockOut;
+        const uint64_t nb = mn64(p.ctr->n_list[kListBig], p.list_cap[kListBig]);
+        const uint64_t nt = mn64(p.ctr->need_tasks, p.task_cap);
+        s.nbt[0] = (nb + kBigCellsPerTask - 1) / kBigCellsPerTask;
+        s.nbt[1] = (nt + kPairWarps - 1) / kPairWarps;
     }
     __syncthreads();
-    uint64_t total = 0;
-#pragma unroll
-    for (int c = 0; c < kNumLists; c++) total += s.nbt[c];
-    const uint32_t slot0 = warp * 64;
+    const uint64_t total = s.nbt[0] + s.nbt[1];
     for (uint64_t bt = blockIdx.x; bt < total; bt += gridDim.x) {
-        uint64_t rem = bt;
-        int cls = 0;
-        while (cls < kNumLists - 1 && rem >= s.nbt[cls]) { rem -= s.nbt[cls]; cls++; }
-        switch (cls) {
-            case 0: small_item<D, 4, BIP, NARROW>(p, s, 0, rem * kPairWarps + warp, slot0); break;
-            case 1: small_item<D, 8, BIP, NARROW>(p, s, 1, rem * kPairWarps + warp, slot0); break;
-            case 2: small_item<D, 16, BIP, NARROW>(p, s, 2, rem * kPairWarps + warp, slot0); break;
-            case 3: small_item<D, 32, BIP, NARROW>(p, s, 3, rem * kPairWarps + warp, slot0); break;
-            case kListBig: big_task<D, BIP, NARROW>(p, s, rem); break;
-            default: huge_item<D, BIP, NARROW>(p, s, rem * kPairWarps + warp, slot0); break;
-        }
+        if (bt < s.nbt[0]) big_task<D, BIP, NARROW>(p, s, bt);
+        else huge_item<D, BIP, NARROW>(p, s, (bt - s.nbt[0]) * kPairWarps + warp, warp * 64);
         __syncthreads();
         const uint32_t on = s.out_n, ovf = s.first_ovf;
         const uint32_t nv = min(on, ovf);
         const bool last = bt + gridDim.x >= total;
-        if (nv >= kFlushAt || on > nv || (last && on > 0)) {
+        if (nv >= kBlockOut / 2 || on > nv || (last && on > 0)) {
             if (t == 0) s.gbase = nv ? atomicAdd(&p.ctr->pairs, (unsigned long long)nv) : 0ull;
             __syncthreads();
             const unsigned long long gb = s.gbase;
@@ -788,7 +908,7 @@ __global__ void __launch_bounds__(kPairThreads, 3) k_pairs(Params p) {
             __syncthreads();
             if (t == 0) {
                 s.out_n = 0;
-                s.first_ovf = kOutBuf;
+                s.first_ovf = kBlockOut;
             }
             __syncthreads();
         }
@@ -822,33 +942,39 @@ __global__ void k_scene_hist(Params p, unsigned long long* hist, unsigned long l
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-static int g_pair_blocks_per_sm = 0;
+static int g_blocks_small = 1, g_blocks_med = 1, g_blocks_block = 1;
 
-size_t pair_smem_bytes() { return sizeof(PairSmem); }
+static size_t med_smem() { return (size_t)kPairWarps * (2 * kMedSlots * sizeof(uint4) + kWarpOut * sizeof(uint2)); }
 
-cudaError_t kernels_init() {
-    const int sm = (int)sizeof(PairSmem);
-    cudaError_t e;
-#define SET_SMEM(K)                                                                             \
-    e = cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);               \
+size_t pair_smem_bytes() { return sizeof(BlockSmem); }
+
+template <int D, bool B, bool N>
+static cudaError_t init_variant() {
+    cudaError_t e = cudaFuncSetAttribute(k_pairs_med<D, B, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)med_smem());
     if (e != cudaSuccess) return e;
-    SET_SMEM((k_pairs<2, false, true>));
-    SET_SMEM((k_pairs<3, false, true>));
-    SET_SMEM((k_pairs<2, true, true>));
-    SET_SMEM((k_pairs<3, true, true>));
-    SET_SMEM((k_pairs<2, false, false>));
-    SET_SMEM((k_pairs<3, false, false>));
-    SET_SMEM((k_pairs<2, true, false>));
-    SET_SMEM((k_pairs<3, true, false>));
-#undef SET_SMEM
-    int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs<3, false, true>, kPairThreads, sm);
-    if (e != cudaSuccess) return e;
-    g_pair_blocks_per_sm = nb > 0 ? nb : 1;
-    return cudaSuccess;
+    e = cudaFuncSetAttribute(k_pairs_block<D, B, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BlockSmem));
+    return e;
 }
 
-int pair_blocks_per_sm() { return g_pair_blocks_per_sm > 0 ? g_pair_blocks_per_sm : 1; }
+cudaError_t kernels_init() {
+    cudaError_t e;
+    if ((e = init_variant<2, false, true>()) != cudaSuccess) return e;
+    if ((e = init_variant<3, false, true>()) != cudaSuccess) return e;
+    if ((e = init_variant<2, true, true>()) != cudaSuccess) return e;
+    if ((e = init_variant<3, true, true>()) != cudaSuccess) return e;
+    if ((e = init_variant<2, false, false>()) != cudaSuccess) return e;
+    if ((e = init_variant<3, false, false>()) != cudaSuccess) return e;
+    if ((e = init_variant<2, true, false>()) != cudaSuccess) return e;
+    if ((e = init_variant<3, true, false>()) != cudaSuccess) return e;
+    int nb = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs_small<3, false, true>, kPairThreads, 0)) != cudaSuccess) return e;
+    g_blocks_small = nb > 0 ? nb : 1;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs_med<3, false, true>, kPairThreads, med_smem())) != cudaSuccess) return e;
+    g_blocks_med = nb > 0 ? nb : 1;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs_block<3, false, true>, kPairThreads, sizeof(BlockSmem))) != cudaSuccess) return e;
+    g_blocks_block = nb > 0 ? nb : 1;
+    return cudaSuccess;
+}
 
 cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st) {
     const unsigned long long n = p.out_cap;
@@ -887,20 +1013,23 @@ cudaError_t launch_expand(const Params& p, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_pairs(const Params& p, int dims, int grid_blocks, cudaStream_t st) {
-    const size_t sm = sizeof(PairSmem);
+template <int D, bool B, bool N>
+static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st) {
+    k_pairs_small<D, B, N><<<sm_count * g_blocks_small, kPairThreads, 0, st>>>(p);
+    k_pairs_med<D, B, N><<<sm_count * g_blocks_med, kPairThreads, med_smem(), st>>>(p);
+    k_pairs_block<D, B, N><<<sm_count * g_blocks_block, kPairThreads, sizeof(BlockSmem), st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st) {
     const bool bip = p.split != kNoSplit;
     const bool narrow = p.max_range <= (1u << kMissShift);
-#define LAUNCH(D, B, N) k_pairs<D, B, N><<<grid_blocks, kPairThreads, sm, st>>>(p)
     if (narrow) {
-        if (dims == 2) { if (bip) LAUNCH(2, true, true); else LAUNCH(2, false, true); }
-        else { if (bip) LAUNCH(3, true, true); else LAUNCH(3, false, true); }
-    } else {
-        if (dims == 2) { if (bip) LAUNCH(2, true, false); else LAUNCH(2, false, false); }
-        else { if (bip) LAUNCH(3, true, false); else LAUNCH(3, false, false); }
+        if (dims == 2) return bip ? launch_pairs_t<2, true, true>(p, sm_count, st) : launch_pairs_t<2, false, true>(p, sm_count, st);
+        return bip ? launch_pairs_t<3, true, true>(p, sm_count, st) : launch_pairs_t<3, false, true>(p, sm_count, st);
     }
-#undef LAUNCH
-    return cudaGetLastError();
+    if (dims == 2) return bip ? launch_pairs_t<2, true, false>(p, sm_count, st) : launch_pairs_t<2, false, false>(p, sm_count, st);
+    return bip ? launch_pairs_t<3, true, false>(p, sm_count, st) : launch_pairs_t<3, false, false>(p, sm_count, st);
 }
 
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,

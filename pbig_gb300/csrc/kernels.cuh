@@ -23,11 +23,14 @@ constexpr uint32_t kNoSplit = 0xffffffffu;
 constexpr int kIdBits = 29;
 constexpr uint32_t kIdMask = (1u << kIdBits) - 1u;
 
-// class lists built by the scan: cells with 2..4, 5..8, 9..16, 17..32 boxes
-// (warp-packed), 33..kBigMax (block-staged) and larger (tiled)
-constexpr int kNumLists = 6;
-constexpr int kListBig = 4, kListHuge = 5;
-constexpr uint32_t kBigMax = 512;   // largest cell staged whole in shared memory
+// class lists built by the scan, one {start, n} record per cell: cells with
+// 2..4, 5..8, 9..16, 17..32 boxes (several per warp), 33..kMedMax (one per
+// warp, staged whole), kMedMax+1..kBigMax (one block, staged whole) and
+// larger (32x32 tile tasks)
+constexpr int kNumLists = 7;
+constexpr int kListMed = 4, kListBig = 5, kListHuge = 6;
+constexpr uint32_t kMedMax = 128;   // largest cell staged by one warp
+constexpr uint32_t kBigMax = 512;   // largest cell staged by one block
 
 struct Scene {
     uint32_t box_off;   // first box of the scene (global index)
@@ -66,10 +69,10 @@ struct Params {
     uint64_t ncells;
     uint32_t* entries;            // [entry_cap]: flags<<29 | global box index
     uint64_t entry_cap;
-    uint32_t* lists;              // kNumLists regions
+    uint2* lists;                 // kNumLists regions of {start, n}
     uint64_t list_off[kNumLists]; // region offsets into lists
     uint64_t list_cap[kNumLists];
-    uint4* tasks;                 // huge-cell tile tasks {cell, r, x0, x1}
+    uint4* tasks;                 // huge-cell tile tasks {start, n, r, x0}
     uint64_t task_cap;
     unsigned long long* tile_state; // scan look-back state, one per tile
     uint2* out;                   // pairs
@@ -82,12 +85,11 @@ cudaError_t launch_count(const Params& p, int dims, cudaStream_t st);
 cudaError_t launch_scan(const Params& p, cudaStream_t st);
 cudaError_t launch_expand(const Params& p, cudaStream_t st);
 cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st);
-cudaError_t launch_pairs(const Params& p, int dims, int grid_blocks, cudaStream_t st);
+cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st);
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,
                                   unsigned long long* scene_cursor, uint2* dst, cudaStream_t st);
 cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st);
 uint64_t scan_tiles(uint64_t ncells);
-int pair_blocks_per_sm();
 size_t pair_smem_bytes();
 cudaError_t kernels_init();
 
