@@ -133,6 +133,25 @@ PBIG2_API int pbig2_host_free(void* ptr);
 
 PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
 
+/* Allocation-free self-intersection (no counterpart in the reference).
+ * For callers that cannot allocate device memory during the query -- a
+ * process whose device memory is owned by another allocator, or a
+ * latency-critical loop that cannot afford cudaMalloc/cudaFree and their
+ * device-wide synchronization. Boxes and the output pairs (pair_cap uint32
+ * pairs, a<b) are caller-owned device buffers; every intermediate buffer
+ * lives in a fixed 16 MiB scratch array inside the library, held by every
+ * GPU that loads the library until exit. Limits: n <= 262144 boxes, a grid
+ * of at most 2^20 cells (the cell size is coarsened to fit) and at most
+ * 524288 box-in-cell entries; larger queries return PBIG2_ECAPACITY. The
+ * scratch is shared by all calls, so calls that overlap on the GPU race; the
+ * first call on a device sets the device up and should come before any
+ * stream capture. *npairs receives the pair count (also when the pair
+ * buffer is too small). Error text: pbig2_noalloc_last_error(). */
+PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, uint32_t dims, uint32_t range,
+                                           uint32_t cell_shift, uint32_t* d_pairs, uint64_t pair_cap,
+                                           uint64_t* npairs, void* stream);
+PBIG2_API const char* pbig2_noalloc_last_error(void);
+
 /* Cell-size autotuner: the shift the engine would pick for these boxes
  * (host memory), from a sample of at most `sample` boxes. */
 PBIG2_API int pbig2_tune_shift(const uint32_t* boxes, uint64_t n, uint32_t dims, uint32_t range,

@@ -27,7 +27,8 @@ EXPORTS = [
     "pbig2_create", "pbig2_destroy", "pbig2_last_error", "pbig2_version", "pbig2_self_intersect",
     "pbig2_bipartite_intersect", "pbig2_batch_intersect", "pbig2_result_pairs", "pbig2_copy_pairs",
     "pbig2_result_scene_offsets", "pbig2_copy_pairs_async", "pbig2_sync", "pbig2_host_alloc",
-    "pbig2_host_free", "pbig2_get_stats", "pbig2_tune_shift",
+    "pbig2_host_free", "pbig2_get_stats", "pbig2_tune_shift", "pbig2_self_intersect_noalloc",
+    "pbig2_noalloc_last_error",
 ]
 
 
@@ -77,6 +78,8 @@ def lib():
         L.pbig2_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
         L.pbig2_host_free.argtypes = [vp]
         L.pbig2_tune_shift.argtypes = [vp, u64, u32, u32, u64, C.POINTER(u32)]
+        L.pbig2_self_intersect_noalloc.argtypes = [vp, u64, u32, u32, u32, vp, u64, C.POINTER(u64), vp]
+        L.pbig2_noalloc_last_error.restype = C.c_char_p
         _LIB = L
     return _LIB
 
