@@ -117,6 +117,46 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
             atomicAdd(&p.ctr->bad, 1u);
         }
     }
+    // warps whose largest box covers few cells walk their boxes' cells per
+    // lane (incremental index arithmetic); warps holding a large box share
+    // the concatenated cell list so that box does not stall its warp
+    uint32_t maxc = cnt;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) maxc = max(maxc, __shfl_xor_sync(FULL_MASK, maxc, o));
+    if (maxc <= 32) {
+        const uint32_t my_box = (uint32_t)gi;
+        uint32_t i = 0, j = 0, k = 0;
+        uint64_t gid = base;
+        const uint64_t row = nrc, plane = (uint64_t)nrc * nrc;
+        for (uint32_t q = 0; q < maxc; q++) {
+            if (q < cnt) {
+                if (SCATTER) {
+                    const uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
+                    const uint32_t st = p.starts[gid];
+                    const uint32_t slot = atomicSub(&p.counts[gid], 1u) - 1u;
+                    const uint64_t pos = (uint64_t)st + slot;
+                    if (pos < p.entry_cap) p.entries[pos] = (f << kIdBits) | my_box;
+                    else atomicOr(&p.ctr->err, kErrEntryOvf);
+                } else {
+                    atomicAdd(&p.counts[gid], 1u);
+                }
+            }
+            // next cell of this box: x fastest, then y, then z
+            i++;
+            gid++;
+            if (i == sx) {
+                i = 0;
+                j++;
+                gid += row - sx;
+                if (j == sy) {
+                    j = 0;
+                    k++;
+                    gid += plane - (uint64_t)sy * row;
+                }
+            }
+        }
+        return;
+    }
     const uint32_t incl = warp_incl_scan(cnt);
     const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
     const uint32_t excl = incl - cnt;
@@ -203,7 +243,7 @@ __device__ __forceinline__ void st_volatile(unsigned long long* a, unsigned long
     *reinterpret_cast<volatile unsigned long long*>(a) = v;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan(Params p) {
+__global__ void __launch_bounds__(kScanThreads, 5) k_scan(Params p) {
     __shared__ uint32_t s_tile;
     __shared__ unsigned long long s_warp_tot[8];
     __shared__ unsigned long long s_prefix;
@@ -288,7 +328,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Params p) {
     const unsigned long long base = s_prefix + warp_excl;
     // write starts and classify cells
     uint32_t my_cls[kNumLists] = {0, 0, 0, 0, 0, 0, 0};
-    uint32_t st_all[16];
     unsigned long long tests = 0;
 #pragma unroll
     for (int r = 0; r < 4; r++) {
@@ -298,7 +337,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Params p) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             st[k] = (uint32_t)run;
-            st_all[4 * r + k] = st[k];
             run += v[4 * r + k];
             const int cl = list_of(v[4 * r + k]);
             if (cl >= 0) my_cls[cl]++;
@@ -334,14 +372,17 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Params p) {
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         const uint64_t c = c_warp + (uint64_t)r * 128 + lane * 4;
+        uint32_t run = (uint32_t)(base + row_excl[r]);
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const int cl = list_of(v[4 * r + k]);
             if (cl >= 0) {
                 const uint64_t idx = (uint64_t)s_cls_base[cl] + atomicAdd(&s_cls[cl], 1u);
-                if (idx < p.list_cap[cl]) p.lists[p.list_off[cl] + idx] = make_uint2(st_all[4 * r + k], v[4 * r + k]);
+                if (idx < p.list_cap[cl]) p.lists[p.list_off[cl] + idx] = make_uint2(run, v[4 * r + k]);
             }
+            run += v[4 * r + k];
         }
+        (void)c;
     }
 }
 
