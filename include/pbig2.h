@@ -139,7 +139,7 @@ PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
  * latency-critical loop that cannot afford cudaMalloc/cudaFree and their
  * device-wide synchronization. Boxes and the output pairs (pair_cap uint32
  * pairs, a<b) are caller-owned device buffers; every intermediate buffer
- * lives in a fixed 16 MiB scratch array inside the library, held by every
+ * lives in a fixed 20 MiB scratch array inside the library, held by every
  * GPU that loads the library until exit. Limits: n <= 262144 boxes, a grid
  * of at most 2^20 cells (the cell size is coarsened to fit) and at most
  * 524288 box-in-cell entries; larger queries return PBIG2_ECAPACITY. The

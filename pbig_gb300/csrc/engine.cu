@@ -296,6 +296,8 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     c->counts_dirty = true;  // until a pass completes, counts may be non-zero
     for (int attempt = 0; attempt < 6; attempt++) {
         CK(c->d_entries.ensure(entry_cap * 4, false, st));
+        CK(c->d_ranks.ensure(c->d_entries.bytes, false, st));
+        CK(c->d_blockbase.ensure(((nboxes + 255) / 256) * 4, false, st));
         // list regions: a cell of class c holds at least lo_c boxes, so with
         // E <= entry capacity no list can overflow
         const uint64_t ecap = c->d_entries.bytes / 4;
@@ -313,6 +315,8 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         p.starts = c->d_starts.as<uint32_t>();
         p.entries = c->d_entries.as<uint32_t>();
         p.entry_cap = c->d_entries.bytes / 4;
+        p.ranks = c->d_ranks.as<uint32_t>();
+        p.block_base = c->d_blockbase.as<uint32_t>();
         p.lists = c->d_lists.as<uint2>();
         p.tasks = c->d_tasks.as<uint4>();
         p.task_cap = c->d_tasks.bytes / 16;
@@ -349,7 +353,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
             return fail(PBIG2_ECUDA, "pipeline failed: %s", cudaGetErrorString(e));
         }
         memcpy(&h, c->h_ctr.p, sizeof(Ctr));
-        c->counts_dirty = false;  // the scatter returned every count to zero
+        c->counts_dirty = false;  // the scan returned every count to zero
         if (h.err & kErrWait) {
             c->counts_dirty = true;
             return fail(PBIG2_ETIMEOUT, "scan look-back wait gave up");
@@ -508,7 +512,8 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     if (!c) return PBIG2_OK;
     cudaSetDevice(c->device);
     if (c->own_stream) cudaStreamSynchronize(c->own_stream);
-    for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_starts, &c->d_entries, &c->d_lists, &c->d_tasks, &c->d_state,
+    for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_starts, &c->d_entries, &c->d_ranks, &c->d_blockbase,
+                      &c->d_lists, &c->d_tasks, &c->d_state,
                       &c->d_out, &c->d_out2, &c->d_ctr, &c->d_scenes, &c->d_scene_off, &c->d_scene_pair,
                       &c->d_scene_cursor})
         b->release();

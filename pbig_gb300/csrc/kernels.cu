@@ -78,11 +78,18 @@ __device__ __forceinline__ void stage_boxes(const Params& p, uint64_t b0, uint32
     }
 }
 
+// Entries of a block of boxes are numbered box by box (thread order), and
+// within a box x fastest, then y, then z. The count pass records each
+// entry's slot in its cell -- the value its atomicAdd returned -- at
+// ranks[block_base + number], block_base being reserved per block; the
+// scatter replays the same numbering and writes without atomics.
 template <int D, bool SCATTER>
 __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t* sbox, uint64_t b0,
                                                 uint32_t nb) {
+    __shared__ uint32_t s_warp_tot[kBoxThreads / 32];
+    __shared__ uint32_t s_block_base;
     constexpr uint32_t W = 2 * D + 1;
-    const uint32_t t = threadIdx.x, lane = t & 31u;
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const uint64_t gi = b0 + t;
     uint32_t cnt = 0, sx = 1, sy = 1, nrc = 0;
     uint64_t base = 0;
@@ -104,7 +111,7 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
             sy = (b[3] >> sh) - lo1 + 1;
             const uint32_t sz = D == 3 ? (b[5] >> sh) - lo2 + 1 : 1u;
             const uint64_t c64 = (uint64_t)sx * sy * sz;
-            if (c64 >= (1ull << 26)) {
+            if (c64 >= (1ull << 22)) {
                 err |= kErrCellOvf;
             } else {
                 cnt = (uint32_t)c64;
@@ -117,6 +124,31 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
             atomicAdd(&p.ctr->bad, 1u);
         }
     }
+    // block-wide numbering of the entries
+    const uint32_t incl = warp_incl_scan(cnt);
+    const uint32_t wtot = __shfl_sync(FULL_MASK, incl, 31);
+    if (lane == 31) s_warp_tot[warp] = wtot;
+    __syncthreads();
+    uint32_t woff = 0, btot = 0;
+#pragma unroll
+    for (uint32_t w = 0; w < kBoxThreads / 32; w++) {
+        const uint32_t x = s_warp_tot[w];
+        woff += w < warp ? x : 0u;
+        btot += x;
+    }
+    if (t == 0) {
+        if (SCATTER) {
+            s_block_base = p.block_base[blockIdx.x];
+        } else {
+            const uint32_t bb = atomicAdd(&p.ctr->rank_cursor, btot);
+            p.block_base[blockIdx.x] = bb;
+            s_block_base = bb;
+        }
+    }
+    __syncthreads();
+    const uint64_t rbase = (uint64_t)s_block_base + woff;  // this warp's first entry
+    const uint32_t excl = incl - cnt;
+
     // warps whose largest box covers few cells walk their boxes' cells per
     // lane (incremental index arithmetic); warps holding a large box share
     // the concatenated cell list so that box does not stall its warp
@@ -128,17 +160,18 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
         uint32_t i = 0, j = 0, k = 0;
         uint64_t gid = base;
         const uint64_t row = nrc, plane = (uint64_t)nrc * nrc;
+        const uint64_t r0 = rbase + excl;
         for (uint32_t q = 0; q < maxc; q++) {
             if (q < cnt) {
+                const uint64_t ri = r0 + q;
                 if (SCATTER) {
                     const uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
-                    const uint32_t st = p.starts[gid];
-                    const uint32_t slot = atomicSub(&p.counts[gid], 1u) - 1u;
-                    const uint64_t pos = (uint64_t)st + slot;
+                    const uint64_t pos = ri < p.entry_cap ? (uint64_t)p.starts[gid] + p.ranks[ri] : ~0ull;
                     if (pos < p.entry_cap) p.entries[pos] = (f << kIdBits) | my_box;
                     else atomicOr(&p.ctr->err, kErrEntryOvf);
                 } else {
-                    atomicAdd(&p.counts[gid], 1u);
+                    const uint32_t slot = atomicAdd(&p.counts[gid], 1u);
+                    if (ri < p.entry_cap) p.ranks[ri] = slot;
                 }
             }
             // next cell of this box: x fastest, then y, then z
@@ -157,11 +190,8 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
         }
         return;
     }
-    const uint32_t incl = warp_incl_scan(cnt);
-    const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
-    const uint32_t excl = incl - cnt;
     const uint64_t wbox0 = b0 + (t & ~31u);
-    for (uint32_t q0 = 0; q0 < total; q0 += 32) {
+    for (uint32_t q0 = 0; q0 < wtot; q0 += 32) {
         const uint32_t q = q0 + lane;
         uint32_t o = 0;  // owner lane: number of lanes whose inclusive count <= q
 #pragma unroll
@@ -174,19 +204,20 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
         const uint32_t o_sy = __shfl_sync(FULL_MASK, sy, o);
         const uint32_t o_nrc = __shfl_sync(FULL_MASK, nrc, o);
         const uint64_t o_base = __shfl_sync(FULL_MASK, base, o);
-        if (q < total) {
+        if (q < wtot) {
             const uint32_t lq = q - o_excl;
             const uint32_t i = lq % o_sx, rr = lq / o_sx;
             const uint32_t j = rr % o_sy, k = rr / o_sy;
             const uint64_t gid = o_base + ((uint64_t)k * o_nrc + j) * o_nrc + i;
+            const uint64_t ri = rbase + q;
             if (SCATTER) {
                 const uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
-                const uint32_t slot = atomicSub(&p.counts[gid], 1u) - 1u;
-                const uint64_t pos = (uint64_t)p.starts[gid] + slot;
+                const uint64_t pos = ri < p.entry_cap ? (uint64_t)p.starts[gid] + p.ranks[ri] : ~0ull;
                 if (pos < p.entry_cap) p.entries[pos] = (f << kIdBits) | (uint32_t)(wbox0 + o);
                 else atomicOr(&p.ctr->err, kErrEntryOvf);
             } else {
-                atomicAdd(&p.counts[gid], 1u);
+                const uint32_t slot = atomicAdd(&p.counts[gid], 1u);
+                if (ri < p.entry_cap) p.ranks[ri] = slot;
             }
         }
     }
@@ -265,11 +296,16 @@ __global__ void __launch_bounds__(kScanThreads, 5) k_scan(Params p) {
     for (int r = 0; r < 4; r++) {
         const uint64_t c = c_warp + (uint64_t)r * 128 + lane * 4;
         if (full) {
-            const uint4 q = __ldcs(reinterpret_cast<const uint4*>(p.counts + c));
+            uint4* a = reinterpret_cast<uint4*>(p.counts + c);
+            const uint4 q = __ldcs(a);
             v[4 * r] = q.x; v[4 * r + 1] = q.y; v[4 * r + 2] = q.z; v[4 * r + 3] = q.w;
+            if (q.x | q.y | q.z | q.w) *a = make_uint4(0u, 0u, 0u, 0u);  // counts start at zero next query
         } else {
 #pragma unroll
-            for (int k = 0; k < 4; k++) v[4 * r + k] = (c + k < p.ncells) ? p.counts[c + k] : 0u;
+            for (int k = 0; k < 4; k++) {
+                v[4 * r + k] = (c + k < p.ncells) ? p.counts[c + k] : 0u;
+                if (v[4 * r + k]) p.counts[c + k] = 0u;
+            }
         }
     }
     // per-row lane sums and warp scans (64-bit running totals)
@@ -302,23 +338,25 @@ __global__ void __launch_bounds__(kScanThreads, 5) k_scan(Params p) {
             long long look = (long long)tile - 1;
             uint32_t spins = 0;
             for (;;) {
-                const long long idx = look - (long long)lane;
+                const long long idx = look - (long long)lane;  // lane 0: nearest predecessor
                 const unsigned long long s = idx >= 0 ? ld_volatile(&p.tile_state[idx]) : kFlagPre;
-                if (__any_sync(FULL_MASK, (s >> 62) == 0)) {
-                    if (++spins > kSpinLimit) {
-                        if (lane == 0) atomicOr(&p.ctr->err, kErrWait);
-                        break;
-                    }
+                const uint32_t notready = __ballot_sync(FULL_MASK, (s >> 62) == 0);
+                const uint32_t pm = __ballot_sync(FULL_MASK, (s >> 62) == 2);
+                // done at the nearest inclusive prefix once every nearer tile has
+                // published its aggregate; a window without one is summed whole
+                const uint32_t first = pm ? (uint32_t)(__ffs(pm) - 1) : 32u;
+                const uint32_t need = first == 32u ? 0xffffffffu : ((1u << first) - 1u);
+                if ((notready & need) == 0) {
+                    excl += warp_sum_u64(lane <= first ? (s & kValMask) : 0ull);
+                    if (pm) break;
+                    look -= 32;
                     continue;
                 }
-                const uint32_t pm = __ballot_sync(FULL_MASK, (s >> 62) == 2);
-                if (pm) {
-                    const uint32_t first = __ffs(pm) - 1;
-                    excl += warp_sum_u64(lane <= first ? (s & kValMask) : 0ull);
+                if (++spins > kSpinLimit) {
+                    if (lane == 0) atomicOr(&p.ctr->err, kErrWait);
                     break;
                 }
-                excl += warp_sum_u64(s & kValMask);
-                look -= 32;
+                __nanosleep(64);
             }
             if (lane == 0) st_volatile(&p.tile_state[tile], kFlagPre | (excl + agg));
         }

@@ -50,7 +50,7 @@ struct Ctr {
     unsigned int n_list[kNumLists];     // class list sizes
     unsigned int n_tasks;               // tile tasks written for huge cells
     unsigned int need_tasks;            // tile tasks needed
-    unsigned int pad;
+    unsigned int rank_cursor;           // entries numbered by the count pass
     unsigned long long entries;         // E
     unsigned long long pairs;           // pairs found (may exceed capacity)
     unsigned long long tests;           // sum of n(n-1)/2 over cells
@@ -64,11 +64,13 @@ struct Params {
     uint32_t nscenes;
     uint32_t split;               // bipartite: global index of the first blue box
     uint32_t max_range;           // largest scene range (selects the pair-test arithmetic)
-    uint32_t* counts;             // [ncells] (zero before count; zero after scatter)
+    uint32_t* counts;             // [ncells] (zero before count; the scan zeroes them again)
     uint32_t* starts;             // [ncells+1] exclusive scan of counts
     uint64_t ncells;
     uint32_t* entries;            // [entry_cap]: flags<<29 | global box index
     uint64_t entry_cap;
+    uint32_t* ranks;              // [entry_cap]: slot of each entry in its cell (count pass)
+    uint32_t* block_base;         // [ceil(nboxes/256)]: first entry number of each box block
     uint2* lists;                 // kNumLists regions of {start, n}
     uint64_t list_off[kNumLists]; // region offsets into lists
     uint64_t list_cap[kNumLists];
