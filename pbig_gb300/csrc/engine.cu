@@ -297,7 +297,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     for (int attempt = 0; attempt < 6; attempt++) {
         CK(c->d_entries.ensure(entry_cap * 4, false, st));
         CK(c->d_ranks.ensure(c->d_entries.bytes, false, st));
-        CK(c->d_blockbase.ensure(((nboxes + 255) / 256) * 4, false, st));
+        CK(c->d_blockbase.ensure(((nboxes + 255) / 256) * 8, false, st));
         // list regions: a cell of class c holds at least lo_c boxes, so with
         // E <= entry capacity no list can overflow
         const uint64_t ecap = c->d_entries.bytes / 4;
@@ -316,7 +316,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         p.entries = c->d_entries.as<uint32_t>();
         p.entry_cap = c->d_entries.bytes / 4;
         p.ranks = c->d_ranks.as<uint32_t>();
-        p.block_base = c->d_blockbase.as<uint32_t>();
+        p.block_base = c->d_blockbase.as<unsigned long long>();
         p.lists = c->d_lists.as<uint2>();
         p.tasks = c->d_tasks.as<uint4>();
         p.task_cap = c->d_tasks.bytes / 16;

@@ -87,7 +87,7 @@ template <int D, bool SCATTER>
 __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t* sbox, uint64_t b0,
                                                 uint32_t nb) {
     __shared__ uint32_t s_warp_tot[kBoxThreads / 32];
-    __shared__ uint32_t s_block_base;
+    __shared__ unsigned long long s_block_base;
     constexpr uint32_t W = 2 * D + 1;
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const uint64_t gi = b0 + t;
@@ -111,7 +111,7 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
             sy = (b[3] >> sh) - lo1 + 1;
             const uint32_t sz = D == 3 ? (b[5] >> sh) - lo2 + 1 : 1u;
             const uint64_t c64 = (uint64_t)sx * sy * sz;
-            if (c64 >= (1ull << 22)) {
+            if (c64 >= (1ull << 26)) {
                 err |= kErrCellOvf;
             } else {
                 cnt = (uint32_t)c64;
@@ -129,24 +129,24 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
     const uint32_t wtot = __shfl_sync(FULL_MASK, incl, 31);
     if (lane == 31) s_warp_tot[warp] = wtot;
     __syncthreads();
-    uint32_t woff = 0, btot = 0;
+    unsigned long long woff = 0, btot = 0;  // a box covers < 2^26 cells: warp sums fit 32 bits
 #pragma unroll
     for (uint32_t w = 0; w < kBoxThreads / 32; w++) {
-        const uint32_t x = s_warp_tot[w];
-        woff += w < warp ? x : 0u;
+        const unsigned long long x = s_warp_tot[w];
+        woff += w < warp ? x : 0ull;
         btot += x;
     }
     if (t == 0) {
         if (SCATTER) {
             s_block_base = p.block_base[blockIdx.x];
         } else {
-            const uint32_t bb = atomicAdd(&p.ctr->rank_cursor, btot);
+            const unsigned long long bb = atomicAdd(&p.ctr->rank_cursor, btot);
             p.block_base[blockIdx.x] = bb;
             s_block_base = bb;
         }
     }
     __syncthreads();
-    const uint64_t rbase = (uint64_t)s_block_base + woff;  // this warp's first entry
+    const uint64_t rbase = s_block_base + woff;  // this warp's first entry
     const uint32_t excl = incl - cnt;
 
     // warps whose largest box covers few cells walk their boxes' cells per

@@ -50,10 +50,11 @@ struct Ctr {
     unsigned int n_list[kNumLists];     // class list sizes
     unsigned int n_tasks;               // tile tasks written for huge cells
     unsigned int need_tasks;            // tile tasks needed
-    unsigned int rank_cursor;           // entries numbered by the count pass
+    unsigned int pad;
     unsigned long long entries;         // E
     unsigned long long pairs;           // pairs found (may exceed capacity)
     unsigned long long tests;           // sum of n(n-1)/2 over cells
+    unsigned long long rank_cursor;     // entries numbered by the count pass
 };
 
 struct Params {
@@ -70,7 +71,7 @@ struct Params {
     uint32_t* entries;            // [entry_cap]: flags<<29 | global box index
     uint64_t entry_cap;
     uint32_t* ranks;              // [entry_cap]: slot of each entry in its cell (count pass)
-    uint32_t* block_base;         // [ceil(nboxes/256)]: first entry number of each box block
+    unsigned long long* block_base; // [ceil(nboxes/256)]: first entry number of each box block
     uint2* lists;                 // kNumLists regions of {start, n}
     uint64_t list_off[kNumLists]; // region offsets into lists
     uint64_t list_cap[kNumLists];

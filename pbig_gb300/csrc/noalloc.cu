@@ -140,7 +140,7 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
     p.entries = (uint32_t*)take(kNaMaxEntries * 4);
     p.entry_cap = kNaMaxEntries;
     p.ranks = (uint32_t*)take(kNaMaxEntries * 4);
-    p.block_base = (uint32_t*)take(((kNaMaxBoxes + 255) / 256) * 4);
+    p.block_base = (unsigned long long*)take(((kNaMaxBoxes + 255) / 256) * 8);
     const uint64_t lo[kNumLists] = {2, 5, 9, 17, 33, kMedMax + 1, kBigMax + 1};
     uint64_t loff = 0;
     for (int k = 0; k < kNumLists; k++) {
