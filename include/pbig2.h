@@ -67,8 +67,10 @@ typedef struct {
     uint32_t reserved;
     double device_ms;      /* device time of the query (CUDA events) */
     /* device time per phase of the last pipeline pass (CUDA events on the
-     * query's stream): count, scan, expand, scatter, pair test, grouping */
-    double phase_ms[6];
+     * query's stream): count, scan, expand, scatter, pair test (all three
+     * pair kernels), grouping by scene, and within the pair test: the
+     * small-cell, medium-cell and block kernels */
+    double phase_ms[9];
 } pbig2_stats;
 
 /* Context: one device, owns its buffers and streams. Not thread-safe; use
@@ -139,7 +141,7 @@ PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
  * latency-critical loop that cannot afford cudaMalloc/cudaFree and their
  * device-wide synchronization. Boxes and the output pairs (pair_cap uint32
  * pairs, a<b) are caller-owned device buffers; every intermediate buffer
- * lives in a fixed 20 MiB scratch array inside the library, held by every
+ * lives in a fixed 16 MiB scratch array inside the library, held by every
  * GPU that loads the library until exit. Limits: n <= 262144 boxes, a grid
  * of at most 2^20 cells (the cell size is coarsened to fit) and at most
  * 524288 box-in-cell entries; larger queries return PBIG2_ECAPACITY. The

@@ -296,8 +296,6 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     c->counts_dirty = true;  // until a pass completes, counts may be non-zero
     for (int attempt = 0; attempt < 6; attempt++) {
         CK(c->d_entries.ensure(entry_cap * 4, false, st));
-        CK(c->d_ranks.ensure(c->d_entries.bytes, false, st));
-        CK(c->d_blockbase.ensure(((nboxes + 255) / 256) * 8, false, st));
         // list regions: a cell of class c holds at least lo_c boxes, so with
         // E <= entry capacity no list can overflow
         const uint64_t ecap = c->d_entries.bytes / 4;
@@ -315,8 +313,6 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         p.starts = c->d_starts.as<uint32_t>();
         p.entries = c->d_entries.as<uint32_t>();
         p.entry_cap = c->d_entries.bytes / 4;
-        p.ranks = c->d_ranks.as<uint32_t>();
-        p.block_base = c->d_blockbase.as<unsigned long long>();
         p.lists = c->d_lists.as<uint2>();
         p.tasks = c->d_tasks.as<uint4>();
         p.task_cap = c->d_tasks.bytes / 16;
@@ -342,7 +338,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
             CK(cudaMemsetAsync(&p.ctr->pairs, 0, sizeof(unsigned long long), st));
             CK(cudaMemsetAsync(&p.ctr->err, 0, sizeof(unsigned int), st));
         }
-        CK(launch_pairs(p, dims, c->sm_count, st));
+        CK(launch_pairs(p, dims, c->sm_count, st, &c->evp[7]));
         launches += 3;
         CK(cudaEventRecord(c->evp[5], st));
         CK(cudaEventRecord(c->ev1, st));
@@ -353,7 +349,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
             return fail(PBIG2_ECUDA, "pipeline failed: %s", cudaGetErrorString(e));
         }
         memcpy(&h, c->h_ctr.p, sizeof(Ctr));
-        c->counts_dirty = false;  // the scan returned every count to zero
+        c->counts_dirty = false;  // the scatter returned every count to zero
         if (h.err & kErrWait) {
             c->counts_dirty = true;
             return fail(PBIG2_ETIMEOUT, "scan look-back wait gave up");
@@ -386,10 +382,16 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-    double phase[6] = {0, 0, 0, 0, 0, 0};
+    double phase[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int k = 0; k < 5; k++) {
         float x = 0;
         if (cudaEventElapsedTime(&x, c->evp[k], c->evp[k + 1]) == cudaSuccess) phase[k] = x;
+    }
+    {
+        float x = 0;
+        if (cudaEventElapsedTime(&x, c->evp[4], c->evp[7]) == cudaSuccess) phase[6] = x;
+        if (cudaEventElapsedTime(&x, c->evp[7], c->evp[8]) == cudaSuccess) phase[7] = x;
+        if (cudaEventElapsedTime(&x, c->evp[8], c->evp[5]) == cudaSuccess) phase[8] = x;
     }
 
     c->npairs = h.pairs;
@@ -438,7 +440,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     s.scenes = nsc;
     s.kernels = (uint32_t)launches;
     s.device_ms = ms;
-    for (int k = 0; k < 6; k++) s.phase_ms[k] = phase[k];
+    for (int k = 0; k < 9; k++) s.phase_ms[k] = phase[k];
     if (h.bad) return fail(PBIG2_EINPUT, "%u boxes violate the input contract (error bits 0x%x) and were skipped",
                            h.bad, h.err);
     return PBIG2_OK;
@@ -498,7 +500,7 @@ PBIG2_API int pbig2_create(int device, pbig2_ctx** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
-    for (int k = 0; k < 7 && e == cudaSuccess; k++) e = cudaEventCreate(&c->evp[k]);
+    for (int k = 0; k < 9 && e == cudaSuccess; k++) e = cudaEventCreate(&c->evp[k]);
     if (e == cudaSuccess) e = kernels_init();
     if (e != cudaSuccess) {
         pbig2_destroy(c);
@@ -512,7 +514,7 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     if (!c) return PBIG2_OK;
     cudaSetDevice(c->device);
     if (c->own_stream) cudaStreamSynchronize(c->own_stream);
-    for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_starts, &c->d_entries, &c->d_ranks, &c->d_blockbase,
+    for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_starts, &c->d_entries,
                       &c->d_lists, &c->d_tasks, &c->d_state,
                       &c->d_out, &c->d_out2, &c->d_ctr, &c->d_scenes, &c->d_scene_off, &c->d_scene_pair,
                       &c->d_scene_cursor})

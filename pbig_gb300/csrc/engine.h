@@ -50,8 +50,8 @@ struct pbig2_ctx {
     int sm_count = 0;
     cudaStream_t own_stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    cudaEvent_t evp[7] = {};
-    pbig::DevBuf d_boxes, d_counts, d_starts, d_entries, d_ranks, d_blockbase, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
+    cudaEvent_t evp[9] = {};
+    pbig::DevBuf d_boxes, d_counts, d_starts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
         d_scenes, d_scene_off, d_scene_pair, d_scene_cursor;
     pbig::HostPinned h_ctr, h_stage;
     bool counts_dirty = false;

@@ -78,18 +78,11 @@ __device__ __forceinline__ void stage_boxes(const Params& p, uint64_t b0, uint32
     }
 }
 
-// Entries of a block of boxes are numbered box by box (thread order), and
-// within a box x fastest, then y, then z. The count pass records each
-// entry's slot in its cell -- the value its atomicAdd returned -- at
-// ranks[block_base + number], block_base being reserved per block; the
-// scatter replays the same numbering and writes without atomics.
 template <int D, bool SCATTER>
 __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t* sbox, uint64_t b0,
                                                 uint32_t nb) {
-    __shared__ uint32_t s_warp_tot[kBoxThreads / 32];
-    __shared__ unsigned long long s_block_base;
     constexpr uint32_t W = 2 * D + 1;
-    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    const uint32_t t = threadIdx.x, lane = t & 31u;
     const uint64_t gi = b0 + t;
     uint32_t cnt = 0, sx = 1, sy = 1, nrc = 0;
     uint64_t base = 0;
@@ -124,74 +117,11 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
             atomicAdd(&p.ctr->bad, 1u);
         }
     }
-    // block-wide numbering of the entries
     const uint32_t incl = warp_incl_scan(cnt);
-    const uint32_t wtot = __shfl_sync(FULL_MASK, incl, 31);
-    if (lane == 31) s_warp_tot[warp] = wtot;
-    __syncthreads();
-    unsigned long long woff = 0, btot = 0;  // a box covers < 2^26 cells: warp sums fit 32 bits
-#pragma unroll
-    for (uint32_t w = 0; w < kBoxThreads / 32; w++) {
-        const unsigned long long x = s_warp_tot[w];
-        woff += w < warp ? x : 0ull;
-        btot += x;
-    }
-    if (t == 0) {
-        if (SCATTER) {
-            s_block_base = p.block_base[blockIdx.x];
-        } else {
-            const unsigned long long bb = atomicAdd(&p.ctr->rank_cursor, btot);
-            p.block_base[blockIdx.x] = bb;
-            s_block_base = bb;
-        }
-    }
-    __syncthreads();
-    const uint64_t rbase = s_block_base + woff;  // this warp's first entry
+    const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
     const uint32_t excl = incl - cnt;
-
-    // warps whose largest box covers few cells walk their boxes' cells per
-    // lane (incremental index arithmetic); warps holding a large box share
-    // the concatenated cell list so that box does not stall its warp
-    uint32_t maxc = cnt;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) maxc = max(maxc, __shfl_xor_sync(FULL_MASK, maxc, o));
-    if (maxc <= 32) {
-        const uint32_t my_box = (uint32_t)gi;
-        uint32_t i = 0, j = 0, k = 0;
-        uint64_t gid = base;
-        const uint64_t row = nrc, plane = (uint64_t)nrc * nrc;
-        const uint64_t r0 = rbase + excl;
-        for (uint32_t q = 0; q < maxc; q++) {
-            if (q < cnt) {
-                const uint64_t ri = r0 + q;
-                if (SCATTER) {
-                    const uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
-                    const uint64_t pos = ri < p.entry_cap ? (uint64_t)p.starts[gid] + p.ranks[ri] : ~0ull;
-                    if (pos < p.entry_cap) p.entries[pos] = (f << kIdBits) | my_box;
-                    else atomicOr(&p.ctr->err, kErrEntryOvf);
-                } else {
-                    const uint32_t slot = atomicAdd(&p.counts[gid], 1u);
-                    if (ri < p.entry_cap) p.ranks[ri] = slot;
-                }
-            }
-            // next cell of this box: x fastest, then y, then z
-            i++;
-            gid++;
-            if (i == sx) {
-                i = 0;
-                j++;
-                gid += row - sx;
-                if (j == sy) {
-                    j = 0;
-                    k++;
-                    gid += plane - (uint64_t)sy * row;
-                }
-            }
-        }
-        return;
-    }
     const uint64_t wbox0 = b0 + (t & ~31u);
-    for (uint32_t q0 = 0; q0 < wtot; q0 += 32) {
+    for (uint32_t q0 = 0; q0 < total; q0 += 32) {
         const uint32_t q = q0 + lane;
         uint32_t o = 0;  // owner lane: number of lanes whose inclusive count <= q
 #pragma unroll
@@ -204,20 +134,19 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
         const uint32_t o_sy = __shfl_sync(FULL_MASK, sy, o);
         const uint32_t o_nrc = __shfl_sync(FULL_MASK, nrc, o);
         const uint64_t o_base = __shfl_sync(FULL_MASK, base, o);
-        if (q < wtot) {
+        if (q < total) {
             const uint32_t lq = q - o_excl;
             const uint32_t i = lq % o_sx, rr = lq / o_sx;
             const uint32_t j = rr % o_sy, k = rr / o_sy;
             const uint64_t gid = o_base + ((uint64_t)k * o_nrc + j) * o_nrc + i;
-            const uint64_t ri = rbase + q;
             if (SCATTER) {
                 const uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
-                const uint64_t pos = ri < p.entry_cap ? (uint64_t)p.starts[gid] + p.ranks[ri] : ~0ull;
+                const uint32_t slot = atomicSub(&p.counts[gid], 1u) - 1u;
+                const uint64_t pos = (uint64_t)p.starts[gid] + slot;
                 if (pos < p.entry_cap) p.entries[pos] = (f << kIdBits) | (uint32_t)(wbox0 + o);
                 else atomicOr(&p.ctr->err, kErrEntryOvf);
             } else {
-                const uint32_t slot = atomicAdd(&p.counts[gid], 1u);
-                if (ri < p.entry_cap) p.ranks[ri] = slot;
+                atomicAdd(&p.counts[gid], 1u);
             }
         }
     }
@@ -296,16 +225,11 @@ __global__ void __launch_bounds__(kScanThreads, 5) k_scan(Params p) {
     for (int r = 0; r < 4; r++) {
         const uint64_t c = c_warp + (uint64_t)r * 128 + lane * 4;
         if (full) {
-            uint4* a = reinterpret_cast<uint4*>(p.counts + c);
-            const uint4 q = __ldcs(a);
+            const uint4 q = __ldcs(reinterpret_cast<const uint4*>(p.counts + c));
             v[4 * r] = q.x; v[4 * r + 1] = q.y; v[4 * r + 2] = q.z; v[4 * r + 3] = q.w;
-            if (q.x | q.y | q.z | q.w) *a = make_uint4(0u, 0u, 0u, 0u);  // counts start at zero next query
         } else {
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                v[4 * r + k] = (c + k < p.ncells) ? p.counts[c + k] : 0u;
-                if (v[4 * r + k]) p.counts[c + k] = 0u;
-            }
+            for (int k = 0; k < 4; k++) v[4 * r + k] = (c + k < p.ncells) ? p.counts[c + k] : 0u;
         }
     }
     // per-row lane sums and warp scans (64-bit running totals)
@@ -1093,22 +1017,24 @@ cudaError_t launch_expand(const Params& p, cudaStream_t st) {
 }
 
 template <int D, bool B, bool N>
-static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st) {
+static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st, cudaEvent_t* ev) {
     k_pairs_small<D, B, N><<<sm_count * g_blocks_small, kPairThreads, 0, st>>>(p);
+    if (ev) cudaEventRecord(ev[0], st);
     k_pairs_med<D, B, N><<<sm_count * g_blocks_med, kPairThreads, med_smem(), st>>>(p);
+    if (ev) cudaEventRecord(ev[1], st);
     k_pairs_block<D, B, N><<<sm_count * g_blocks_block, kPairThreads, sizeof(BlockSmem), st>>>(p);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st) {
+cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev) {
     const bool bip = p.split != kNoSplit;
     const bool narrow = p.max_range <= (1u << kMissShift);
     if (narrow) {
-        if (dims == 2) return bip ? launch_pairs_t<2, true, true>(p, sm_count, st) : launch_pairs_t<2, false, true>(p, sm_count, st);
-        return bip ? launch_pairs_t<3, true, true>(p, sm_count, st) : launch_pairs_t<3, false, true>(p, sm_count, st);
+        if (dims == 2) return bip ? launch_pairs_t<2, true, true>(p, sm_count, st, ev) : launch_pairs_t<2, false, true>(p, sm_count, st, ev);
+        return bip ? launch_pairs_t<3, true, true>(p, sm_count, st, ev) : launch_pairs_t<3, false, true>(p, sm_count, st, ev);
     }
-    if (dims == 2) return bip ? launch_pairs_t<2, true, false>(p, sm_count, st) : launch_pairs_t<2, false, false>(p, sm_count, st);
-    return bip ? launch_pairs_t<3, true, false>(p, sm_count, st) : launch_pairs_t<3, false, false>(p, sm_count, st);
+    if (dims == 2) return bip ? launch_pairs_t<2, true, false>(p, sm_count, st, ev) : launch_pairs_t<2, false, false>(p, sm_count, st, ev);
+    return bip ? launch_pairs_t<3, true, false>(p, sm_count, st, ev) : launch_pairs_t<3, false, false>(p, sm_count, st, ev);
 }
 
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,

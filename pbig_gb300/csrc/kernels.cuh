@@ -54,7 +54,6 @@ struct Ctr {
     unsigned long long entries;         // E
     unsigned long long pairs;           // pairs found (may exceed capacity)
     unsigned long long tests;           // sum of n(n-1)/2 over cells
-    unsigned long long rank_cursor;     // entries numbered by the count pass
 };
 
 struct Params {
@@ -65,13 +64,11 @@ struct Params {
     uint32_t nscenes;
     uint32_t split;               // bipartite: global index of the first blue box
     uint32_t max_range;           // largest scene range (selects the pair-test arithmetic)
-    uint32_t* counts;             // [ncells] (zero before count; the scan zeroes them again)
+    uint32_t* counts;             // [ncells] (zero before count; zero after scatter)
     uint32_t* starts;             // [ncells+1] exclusive scan of counts
     uint64_t ncells;
     uint32_t* entries;            // [entry_cap]: flags<<29 | global box index
     uint64_t entry_cap;
-    uint32_t* ranks;              // [entry_cap]: slot of each entry in its cell (count pass)
-    unsigned long long* block_base; // [ceil(nboxes/256)]: first entry number of each box block
     uint2* lists;                 // kNumLists regions of {start, n}
     uint64_t list_off[kNumLists]; // region offsets into lists
     uint64_t list_cap[kNumLists];
@@ -88,7 +85,9 @@ cudaError_t launch_count(const Params& p, int dims, cudaStream_t st);
 cudaError_t launch_scan(const Params& p, cudaStream_t st);
 cudaError_t launch_expand(const Params& p, cudaStream_t st);
 cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st);
-cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st);
+// ev (optional, 2 events) is recorded after the small-cell and after the
+// medium-cell kernel
+cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev = nullptr);
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,
                                   unsigned long long* scene_cursor, uint2* dst, cudaStream_t st);
 cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st);

@@ -12,7 +12,7 @@
 // call allocates nothing.
 //
 // The scratch array is a file-scope __device__ array of kScratchBytes
-// (20 MiB): every GPU that loads the library holds it until the process
+// (16 MiB): every GPU that loads the library holds it until the process
 // exits. Every call shares it and it keeps the last call's contents, so the
 // call clears what must start at zero; calls that overlap on the GPU (two
 // host threads, or two streams) race on it and must be serialized by the
@@ -30,7 +30,7 @@
 
 namespace pbig {
 
-static constexpr size_t kScratchBytes = 20u << 20;
+static constexpr size_t kScratchBytes = 16u << 20;
 
 // limits of one allocation-free query (so that everything fits the scratch)
 static constexpr uint64_t kNaMaxBoxes = 1u << 18;    // 262,144 boxes
@@ -139,8 +139,6 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
     p.tile_state = (unsigned long long*)take(tiles * 8);
     p.entries = (uint32_t*)take(kNaMaxEntries * 4);
     p.entry_cap = kNaMaxEntries;
-    p.ranks = (uint32_t*)take(kNaMaxEntries * 4);
-    p.block_base = (unsigned long long*)take(((kNaMaxBoxes + 255) / 256) * 8);
     const uint64_t lo[kNumLists] = {2, 5, 9, 17, 33, kMedMax + 1, kBigMax + 1};
     uint64_t loff = 0;
     for (int k = 0; k < kNumLists; k++) {
@@ -151,7 +149,7 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
     p.lists = (uint2*)take(loff * 8);
     p.tasks = (uint4*)take(kNaMaxTasks * 16);
     p.task_cap = kNaMaxTasks;
-    if (off > kScratchBytes) return na_fail(PBIG2_ECAPACITY, "scratch layout exceeds 20 MiB");
+    if (off > kScratchBytes) return na_fail(PBIG2_ECAPACITY, "scratch layout exceeds 16 MiB");
 
     Scene sc{};
     sc.box_off = 0;

@@ -42,9 +42,9 @@ class Stats(C.Structure):
     _fields_ = [("boxes", C.c_uint64), ("bad_boxes", C.c_uint64), ("cells", C.c_uint64),
                 ("entries", C.c_uint64), ("pair_tests", C.c_uint64), ("pairs", C.c_uint64),
                 ("cell_shift", C.c_uint32), ("scenes", C.c_uint32), ("kernels", C.c_uint32),
-                ("reserved", C.c_uint32), ("device_ms", C.c_double), ("phase_ms", C.c_double * 6)]
+                ("reserved", C.c_uint32), ("device_ms", C.c_double), ("phase_ms", C.c_double * 9)]
 
-    PHASES = ("count", "scan", "expand", "scatter", "pairs", "group")
+    PHASES = ("count", "scan", "expand", "scatter", "pairs", "group", "pairs_small", "pairs_med", "pairs_block")
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "phase_ms")}

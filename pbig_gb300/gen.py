@@ -73,11 +73,26 @@ def mixed3d(n: int = 2097152, seed: int = 0, large_frac: float = 0.01) -> np.nda
     return out
 
 
-def scene3d(n: int, seed: int) -> np.ndarray:
-    """One batched/serving scene: uniform centres, sides U[0.5,2]*n^(-1/3)*0.5."""
-    out = np.empty((n, 7), dtype=np.uint32)
+def scene3d(n: int, seed: int, out: np.ndarray | None = None) -> np.ndarray:
+    """One batched/serving scene: uniform centres, sides U[0.5,2]*n^(-1/3)*0.5
+    (written into `out`, a C-contiguous [n,7] uint32 view, when given)."""
+    if out is None:
+        out = np.empty((n, 7), dtype=np.uint32)
+    assert out.shape == (n, 7) and out.dtype == np.uint32 and out.flags.c_contiguous
     _lib().pbig_gen_scene3d(n, seed, _p(out), _threads())
     return out
+
+
+def scene_batch(count: int = 4096, seed: int = 0, lo: int = 256, hi: int = 262144):
+    """Batched-scenes workload: `count` scenes with log-uniform sizes in
+    [lo, hi], scene i generated with seed 1000003*seed + i; returns (boxes
+    concatenated, scene offsets[count+1])."""
+    sizes = scene_sizes(count, seed, lo, hi)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    boxes = np.empty((int(offs[-1]), 7), dtype=np.uint32)
+    for i, n in enumerate(sizes):
+        scene3d(int(n), 1000003 * seed + i, out=boxes[int(offs[i]):int(offs[i + 1])])
+    return boxes, offs
 
 
 def scene_sizes(count: int, seed: int, lo: float, hi: float) -> np.ndarray:
