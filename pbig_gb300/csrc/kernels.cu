@@ -618,7 +618,46 @@ __device__ __forceinline__ void row_unit(const Params& p, const Slots& s, uint32
 
 // ---- small cells ------------------------------------------------------------
 // lane group g (WG lanes) holds cell item*G+g of the class list, lane r its
-// box r; the circular half sweep runs inside the group.
+// box r; the circular half sweep runs inside the group. A warp loads two
+// items before testing either, so their dependent loads (list record, entry,
+// box) overlap.
+template <int D, int WG, bool NARROW>
+__device__ __forceinline__ Box small_fetch(const Params& p, int list, uint64_t nl, uint64_t ci, uint32_t r,
+                                           uint32_t& n) {
+    n = 0;
+    uint32_t start = 0;
+    if (ci < nl) {
+        const uint2 sn = p.lists[p.list_off[list] + ci];
+        start = sn.x;
+        n = sn.y;
+        if (n > WG || (uint64_t)start + n > p.entry_cap) n = 0;  // inconsistent grid: skip
+    }
+    return r < n ? load_box<D, NARROW>(p, p.entries[start + r]) : dummy_box<NARROW>();
+}
+
+template <int D, int WG, bool BIP, bool NARROW>
+__device__ __forceinline__ void small_sweep(const Params& p, const Slots& s, WarpOut& o, const Box& me, uint32_t n,
+                                            uint32_t lane, uint32_t g, uint32_t r) {
+    slot_put(s, lane, me);
+    __syncwarp();
+    const uint32_t gb = g * WG;
+    const uint32_t nelm = r < n ? (r < (n >> 1) ? (n >> 1) : ((n - 1) >> 1)) : 0u;
+    uint32_t mask = 0;
+#pragma unroll
+    for (uint32_t d = 1; d <= WG / 2; d++) {
+        uint32_t pr = r + d;
+        if (pr >= n) pr -= n;
+        if (pr >= WG) pr = 0;  // idle lanes (n = 0) stay inside the group
+        mask |= (hit_bit<D, BIP, NARROW>(me, slot_get(s, gb + pr), p.split) & (d <= nelm ? 1u : 0u)) << d;
+    }
+    auto pid = [&](uint32_t d) {
+        uint32_t pr = r + d;
+        if (pr >= n) pr -= n;
+        return slot_id(s, gb + pr);
+    };
+    wemit<BIP>(p, o, mask, pid, 0u, pid, me.id);
+}
+
 template <int D, int WG, bool BIP, bool NARROW>
 __device__ __forceinline__ void small_items(const Params& p, const Slots& s, WarpOut& o, int list, uint64_t first,
                                             uint64_t stride) {
@@ -626,40 +665,17 @@ __device__ __forceinline__ void small_items(const Params& p, const Slots& s, War
     const uint32_t lane = lane_id(), g = lane / WG, r = lane % WG;
     const uint64_t nl = mn64(p.ctr->n_list[list], p.list_cap[list]);
     const uint64_t nitems = (nl + G - 1) / G;
-    const uint32_t gb = g * WG;
-    for (uint64_t item = first; item < nitems; item += stride) {
-        const uint64_t ci = item * G + g;
-        uint32_t n = 0, start = 0;
-        if (ci < nl) {
-            const uint2 sn = p.lists[p.list_off[list] + ci];
-            start = sn.x;
-            n = sn.y;
-            if (n > WG || (uint64_t)start + n > p.entry_cap) n = 0;  // inconsistent grid: skip
-        }
-        const bool have = r < n;
-        const Box me = have ? load_box<D, NARROW>(p, p.entries[start + r]) : dummy_box<NARROW>();
-        slot_put(s, lane, me);
-        __syncwarp();
-        const uint32_t nelm = have ? (r < (n >> 1) ? (n >> 1) : ((n - 1) >> 1)) : 0u;
-        uint32_t mask = 0;
-#pragma unroll
-        for (uint32_t d = 1; d <= WG / 2; d++) {
-            uint32_t pr = r + d;
-            if (pr >= n) pr -= n;
-            if (pr >= WG) pr = 0;  // idle lanes (n = 0) stay inside the group
-            mask |= (hit_bit<D, BIP, NARROW>(me, slot_get(s, gb + pr), p.split) & (d <= nelm ? 1u : 0u)) << d;
-        }
-        auto pid = [&](uint32_t d) {
-            uint32_t pr = r + d;
-            if (pr >= n) pr -= n;
-            return slot_id(s, gb + pr);
-        };
-        wemit<BIP>(p, o, mask, pid, 0u, pid, me.id);
+    for (uint64_t item = first; item < nitems; item += 2 * stride) {
+        uint32_t n1, n2;
+        const Box a = small_fetch<D, WG, NARROW>(p, list, nl, item * G + g, r, n1);
+        const Box b = small_fetch<D, WG, NARROW>(p, list, nl, (item + stride) * G + g, r, n2);
+        small_sweep<D, WG, BIP, NARROW>(p, s, o, a, n1, lane, g, r);
+        small_sweep<D, WG, BIP, NARROW>(p, s, o, b, n2, lane, g, r);
     }
 }
 
 template <int D, bool BIP, bool NARROW>
-__global__ void __launch_bounds__(kPairThreads, 6) k_pairs_small(Params p) {
+__global__ void __launch_bounds__(kPairThreads, 5) k_pairs_small(Params p) {
     __shared__ uint4 s_a[kPairWarps][kSmallSlots], s_b[kPairWarps][kSmallSlots];
     __shared__ uint2 s_out[kPairWarps][kWarpOut];
     const uint32_t warp = threadIdx.x >> 5;
@@ -922,23 +938,45 @@ __global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
 // group pairs by scene (batched queries): a pair's scene is the scene of its
 // first box; pairs are written to their scene's range with scene-local ids.
 // ---------------------------------------------------------------------------
+// lanes of a warp holding pairs of the same scene share one atomic (pairs
+// come out of the pair kernels in runs of one scene)
+__device__ __forceinline__ unsigned long long warp_scene_reserve(unsigned long long* ctr, uint32_t sc, bool valid,
+                                                                  uint32_t& rank) {
+    const uint32_t lane = lane_id();
+    const uint32_t key = valid ? sc : 0xffffffffu;
+    const uint32_t same = __match_any_sync(FULL_MASK, key);
+    const uint32_t leader = __ffs(same) - 1;
+    rank = __popc(same & ((1u << lane) - 1u));
+    unsigned long long base = 0;
+    if (valid && lane == leader) base = atomicAdd(&ctr[sc], (unsigned long long)__popc(same));
+    return __shfl_sync(FULL_MASK, base, leader);
+}
+
 __global__ void k_group_by_scene(Params p, const unsigned long long* scene_pair_off,
                                  unsigned long long* scene_cursor, uint2* dst, unsigned long long n) {
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        const uint2 pr = p.out[i];
-        const uint32_t sc = find_scene(p, pr.x);
-        const uint32_t off = p.scene_box_off[sc];
-        const unsigned long long k = atomicAdd(&scene_cursor[sc], 1ull);
-        dst[scene_pair_off[sc] + k] = make_uint2(pr.x - off, pr.y - off);
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long n32 = (n + 31) & ~31ull;  // whole warps iterate together
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n32; i += stride) {
+        const bool valid = i < n;
+        const uint2 pr = valid ? p.out[i] : make_uint2(0u, 0u);
+        const uint32_t sc = valid ? find_scene(p, pr.x) : 0u;
+        uint32_t rank;
+        const unsigned long long base = warp_scene_reserve(scene_cursor, sc, valid, rank);
+        if (valid) {
+            const uint32_t off = p.scene_box_off[sc];
+            dst[scene_pair_off[sc] + base + rank] = make_uint2(pr.x - off, pr.y - off);
+        }
     }
 }
 
 __global__ void k_scene_hist(Params p, unsigned long long* hist, unsigned long long n) {
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        const uint32_t sc = find_scene(p, p.out[i].x);
-        atomicAdd(&hist[sc], 1ull);
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long n32 = (n + 31) & ~31ull;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n32; i += stride) {
+        const bool valid = i < n;
+        const uint32_t sc = valid ? find_scene(p, p.out[i].x) : 0u;
+        uint32_t rank;
+        warp_scene_reserve(hist, sc, valid, rank);
     }
 }
 
