@@ -135,6 +135,13 @@ PBIG2_API int pbig2_host_free(void* ptr);
 
 PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
 
+/* Context options. PBIG2_OPT_GRAPH (default 1): batched queries capture
+ * their pipeline (kernels and copies, sizes read from device memory) into a
+ * CUDA graph once, and replay it for later batches with the same box buffer,
+ * dims, range and no more boxes, cells or scenes than the captured one. */
+#define PBIG2_OPT_GRAPH 1
+PBIG2_API int pbig2_set_option(pbig2_ctx* ctx, int option, int64_t value);
+
 /* Allocation-free self-intersection (no counterpart in the reference).
  * For callers that cannot allocate device memory during the query -- a
  * process whose device memory is owned by another allocator, or a

@@ -219,6 +219,170 @@ struct GridScene {
     int grid_of;  // index of the scene whose grid this one shares (self for its own)
 };
 
+// device buffers of one query; fills the matching Params fields
+static int ensure_query_buffers(pbig2_ctx* c, Params& p, uint64_t entry_cap, uint64_t out_cap, uint64_t task_cap,
+                                uint32_t nsc, bool grouped, cudaStream_t st) {
+    CK(c->d_entries.ensure(entry_cap * 4, false, st));
+    // list regions: a cell of class c holds at least lo_c boxes, so with
+    // E <= entry capacity no list can overflow
+    const uint64_t ecap = c->d_entries.bytes / 4;
+    const uint64_t lo[kNumLists] = {2, 5, 9, 17, 33, kMedMax + 1, kBigMax + 1};
+    uint64_t loff = 0;
+    for (int k = 0; k < kNumLists; k++) {
+        p.list_off[k] = loff;
+        p.list_cap[k] = ecap / lo[k] + 1;
+        loff += p.list_cap[k];
+    }
+    CK(c->d_lists.ensure(loff * 8, false, st));
+    CK(c->d_tasks.ensure(task_cap * 16, false, st));
+    CK(c->d_out.ensure(out_cap * 8, false, st));
+    if (grouped) {
+        CK(c->d_out2.ensure(c->d_out.bytes, false, st));
+        CK(c->d_scene_pair.ensure((nsc + 1) * 8, false, st));
+        CK(c->d_scene_cursor.ensure((nsc + 1) * 8, false, st));
+    }
+    p.counts = c->d_counts.as<uint32_t>();
+    p.starts = c->d_starts.as<uint32_t>();
+    p.entries = c->d_entries.as<uint32_t>();
+    p.entry_cap = ecap;
+    p.lists = c->d_lists.as<uint2>();
+    p.tasks = c->d_tasks.as<uint4>();
+    p.task_cap = c->d_tasks.bytes / 16;
+    p.out = c->d_out.as<uint2>();
+    p.out_cap = c->d_out.bytes / 8;
+    return PBIG2_OK;
+}
+
+// the launches of one pipeline pass (also what a graph captures): counters
+// and scan state reset, count, scan, expand, scatter, the three pair
+// kernels and, for batches, grouping of the pairs by scene
+static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool grouped, uint32_t nsc,
+                                   bool full, cudaStream_t st) {
+    cudaError_t e;
+#define R(x)                          \
+    if ((e = (x)) != cudaSuccess) return e;
+    if (full) {
+        R(cudaMemsetAsync(p.ctr, 0, sizeof(Ctr), st));
+        R(cudaMemsetAsync(p.tile_state, 0, scan_tiles(p.ncells) * 8, st));
+        R(cudaEventRecord(c->evp[0], st));
+        R(launch_count(p, dims, st));
+        R(cudaEventRecord(c->evp[1], st));
+        R(launch_scan(p, st));
+        R(cudaEventRecord(c->evp[2], st));
+        R(launch_expand(p, st));
+        R(cudaEventRecord(c->evp[3], st));
+        R(launch_scatter(p, dims, st));
+        R(cudaEventRecord(c->evp[4], st));
+    } else {
+        // keep the grid and lists; clear the pair count and error word
+        R(cudaMemsetAsync(&p.ctr->pairs, 0, sizeof(unsigned long long), st));
+        R(cudaMemsetAsync(&p.ctr->err, 0, sizeof(unsigned int), st));
+        R(cudaEventRecord(c->evp[4], st));
+    }
+    R(launch_pairs(p, dims, c->sm_count, st, &c->evp[7]));
+    R(cudaEventRecord(c->evp[5], st));
+    if (grouped) {
+        unsigned long long* hist = c->d_scene_cursor.as<unsigned long long>();
+        unsigned long long* offs = c->d_scene_pair.as<unsigned long long>();
+        R(cudaMemsetAsync(hist, 0, (nsc + 1) * 8, st));
+        R(launch_scene_hist(p, hist, st));
+        R(launch_scene_offsets(p, hist, offs, nsc, st));
+        R(cudaMemsetAsync(hist, 0, (nsc + 1) * 8, st));
+        R(launch_group_by_scene(p, offs, hist, c->d_out2.as<uint2>(), st));
+    }
+    R(cudaEventRecord(c->ev1, st));
+#undef R
+    return cudaSuccess;
+}
+
+// result bookkeeping after a pass: pair count, per-scene offsets, stats
+static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t ncells, uint32_t nsc,
+                        const std::vector<GridScene>& scenes, bool grouped, int launches, cudaStream_t st) {
+    c->npairs = h.pairs;
+    c->result = grouped ? c->d_out2.as<uint2>() : c->d_out.as<uint2>();
+    if (grouped) {
+        CK(c->h_stage.ensure((nsc + 1) * 8));
+        CK(cudaMemcpyAsync(c->h_stage.p, c->d_scene_pair.p, (nsc + 1) * 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        c->scene_pair_off.assign((const uint64_t*)c->h_stage.p, (const uint64_t*)c->h_stage.p + nsc + 1);
+    } else {
+        c->scene_pair_off.assign(1, 0);
+        c->scene_pair_off.push_back(h.pairs);
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    double phase[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 5; k++) {
+        float x = 0;
+        if (cudaEventElapsedTime(&x, c->evp[k], c->evp[k + 1]) == cudaSuccess) phase[k] = x;
+    }
+    {
+        float x = 0;
+        if (grouped && cudaEventElapsedTime(&x, c->evp[5], c->ev1) == cudaSuccess) phase[5] = x;
+        if (cudaEventElapsedTime(&x, c->evp[4], c->evp[7]) == cudaSuccess) phase[6] = x;
+        if (cudaEventElapsedTime(&x, c->evp[7], c->evp[8]) == cudaSuccess) phase[7] = x;
+        if (cudaEventElapsedTime(&x, c->evp[8], c->evp[5]) == cudaSuccess) phase[8] = x;
+    }
+    pbig2_stats& s = c->stats;
+    s.boxes = nboxes;
+    s.bad_boxes = h.bad;
+    s.cells = ncells;
+    s.entries = h.entries;
+    s.pair_tests = h.tests;
+    s.pairs = h.pairs;
+    s.cell_shift = scenes.empty() ? 0 : scenes[0].shift;
+    s.scenes = nsc;
+    s.kernels = (uint32_t)launches;
+    s.device_ms = ms;
+    for (int k = 0; k < 9; k++) s.phase_ms[k] = phase[k];
+    if (h.bad) return fail(PBIG2_EINPUT, "%u boxes violate the input contract (error bits 0x%x) and were skipped",
+                           h.bad, h.err);
+    return PBIG2_OK;
+}
+
+// capture the pipeline of a batched query (sizes read from device memory,
+// grids and buffers sized for this query) into a graph for later batches
+static int capture_graph(pbig2_ctx* c, const Params& p0, const uint32_t* d_boxes, uint64_t nboxes, uint64_t ncells,
+                         uint32_t nsc, int dims, uint32_t range, uint32_t split, uint64_t entry_cap,
+                         cudaStream_t st) {
+    (void)entry_cap;
+    CK(cudaStreamSynchronize(st));
+    Params p = p0;
+    p.dyn = c->d_dims.as<RunDims>();
+    p.nboxes = nboxes;
+    p.ncells = ncells;
+    p.nscenes = nsc;
+    cudaStream_t cs = c->own_stream;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = record_pipeline(c, p, dims, true, nsc, true, cs);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_ctr.p, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, cs);
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(PBIG2_ECUDA, "graph capture: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(PBIG2_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    c->drop_graph();
+    pbig2_ctx::Graph& G = c->graph;
+    G.exec = ex;
+    G.boxes = d_boxes;
+    G.dims = dims;
+    G.range = range;
+    G.split = split;
+    G.nboxes_cap = nboxes;
+    G.ncells_cap = ncells;
+    G.nscenes_cap = nsc;
+    G.entry_cap = p.entry_cap;
+    G.out_cap = p.out_cap;
+    G.launches = 10;
+    G.buffers = c->buffers_sig();
+    return PBIG2_OK;
+}
+
 static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, int dims, uint32_t range,
                         const std::vector<GridScene>& scenes, uint32_t split, double est_entries,
                         cudaStream_t st, bool group) {
@@ -251,25 +415,70 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     box_off[nsc] = (uint32_t)nboxes;
     if (ncells >= (1ull << 32) - 1)
         return fail(PBIG2_EINVAL, "grid too fine: %llu cells (limit 2^32)", (unsigned long long)ncells);
+    const bool grouped = group && nsc > 1;
 
+    // a captured graph serves this query if the buffers it was captured with
+    // are large enough and the fixed arguments match
+    pbig2_ctx::Graph& G = c->graph;
+    const bool graph_fits = c->use_graph && grouped && G.exec && G.boxes == d_boxes && G.dims == dims &&
+                            G.range == range && G.split == split && nboxes <= G.nboxes_cap &&
+                            ncells <= G.ncells_cap && nsc <= G.nscenes_cap && G.buffers == c->buffers_sig();
+
+    // tables -> pinned staging -> device (before the pipeline or graph)
     const size_t tab_bytes = nsc * sizeof(Scene), off_bytes = (nsc + 1) * sizeof(uint32_t);
-    CK(c->h_stage.ensure(tab_bytes + off_bytes + 64));
+    CK(c->h_stage.ensure(tab_bytes + off_bytes + sizeof(RunDims) + 64));
     CK(cudaStreamSynchronize(st));  // staging buffer reuse
+    RunDims rd{};
+    rd.nboxes = nboxes;
+    rd.ncells = ncells;
+    rd.nscenes = nsc;
     memcpy(c->h_stage.p, tab.data(), tab_bytes);
     memcpy((char*)c->h_stage.p + tab_bytes, box_off.data(), off_bytes);
-    CK(c->d_scenes.ensure(tab_bytes, false, st));
-    CK(c->d_scene_off.ensure(off_bytes, false, st));
+    memcpy((char*)c->h_stage.p + tab_bytes + off_bytes, &rd, sizeof rd);
+    if (!graph_fits) {
+        CK(c->d_scenes.ensure(tab_bytes, false, st));
+        CK(c->d_scene_off.ensure(off_bytes, false, st));
+    }
+    CK(c->d_dims.ensure(sizeof(RunDims), false, st));
     CK(cudaMemcpyAsync(c->d_scenes.p, c->h_stage.p, tab_bytes, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->d_scene_off.p, (char*)c->h_stage.p + tab_bytes, off_bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->d_dims.p, (char*)c->h_stage.p + tab_bytes + off_bytes, sizeof rd, cudaMemcpyHostToDevice,
+                       st));
 
-    // capacities
+    Ctr h{};
+    int launches = 0;
+    if (graph_fits) {
+        CK(cudaGraphLaunch(G.exec, st));
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            c->counts_dirty = true;
+            return fail(PBIG2_ECUDA, "pipeline failed: %s", cudaGetErrorString(e));
+        }
+        memcpy(&h, c->h_ctr.p, sizeof(Ctr));
+        launches = G.launches;
+        const bool over = (h.err & (kErrEntryOvf | kErrTaskOvf | kErrOutOvf)) || h.entries > G.entry_cap ||
+                          h.pairs > G.out_cap;
+        if (h.err & kErrWait) {
+            c->counts_dirty = true;
+            return fail(PBIG2_ETIMEOUT, "scan look-back wait gave up");
+        }
+        if (over) {
+            // the counts went back to zero; redo eagerly with larger buffers
+            // and capture again next time
+            c->drop_graph();
+            c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
+            est_entries = std::max(est_entries, (double)h.entries * 1.1);
+        } else {
+            return finish_query(c, h, nboxes, ncells, nsc, scenes, grouped, launches, st);
+        }
+    }
+
+    // ---- eager run (retries on capacity) ----
     const bool counts_new = c->d_counts.bytes < ncells * 4;
     CK(c->d_counts.ensure(ncells * 4, true, st));
     if (c->counts_dirty && !counts_new) CK(cudaMemsetAsync(c->d_counts.p, 0, c->d_counts.bytes, st));
-    c->counts_dirty = false;
     CK(c->d_starts.ensure((ncells + 1) * 4 + 16, false, st));
-    const uint64_t tiles = scan_tiles(ncells);
-    CK(c->d_state.ensure(tiles * 8, false, st));
+    CK(c->d_state.ensure(scan_tiles(ncells) * 8, false, st));
     CK(c->d_ctr.ensure(sizeof(Ctr), false, st));
     CK(c->h_ctr.ensure(sizeof(Ctr)));
 
@@ -290,58 +499,16 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     p.ncells = ncells;
     p.tile_state = c->d_state.as<unsigned long long>();
     p.ctr = c->d_ctr.as<Ctr>();
-    Ctr h{};
-    int launches = 0;
-    bool need_full = true;
+    p.dyn = nullptr;
     c->counts_dirty = true;  // until a pass completes, counts may be non-zero
+    bool need_full = true;
     for (int attempt = 0; attempt < 6; attempt++) {
-        CK(c->d_entries.ensure(entry_cap * 4, false, st));
-        // list regions: a cell of class c holds at least lo_c boxes, so with
-        // E <= entry capacity no list can overflow
-        const uint64_t ecap = c->d_entries.bytes / 4;
-        const uint64_t lo[kNumLists] = {2, 5, 9, 17, 33, kMedMax + 1, kBigMax + 1};
-        uint64_t loff = 0;
-        for (int k = 0; k < kNumLists; k++) {
-            p.list_off[k] = loff;
-            p.list_cap[k] = ecap / lo[k] + 1;
-            loff += p.list_cap[k];
-        }
-        CK(c->d_lists.ensure(loff * 8, false, st));
-        CK(c->d_tasks.ensure(task_cap * 16, false, st));
-        CK(c->d_out.ensure(out_cap * 8, false, st));
-        p.counts = c->d_counts.as<uint32_t>();
-        p.starts = c->d_starts.as<uint32_t>();
-        p.entries = c->d_entries.as<uint32_t>();
-        p.entry_cap = c->d_entries.bytes / 4;
-        p.lists = c->d_lists.as<uint2>();
-        p.tasks = c->d_tasks.as<uint4>();
-        p.task_cap = c->d_tasks.bytes / 16;
-        p.out = c->d_out.as<uint2>();
-        p.out_cap = c->d_out.bytes / 8;
+        int rc = ensure_query_buffers(c, p, entry_cap, out_cap, task_cap, nsc, grouped, st);
+        if (rc) return rc;
         if (attempt == 0) CK(cudaEventRecord(c->ev0, st));
-        if (need_full) {
-            CK(cudaMemsetAsync(p.ctr, 0, sizeof(Ctr), st));
-            CK(cudaMemsetAsync(p.tile_state, 0, tiles * 8, st));
-            CK(cudaEventRecord(c->evp[0], st));
-            CK(launch_count(p, dims, st));
-            CK(cudaEventRecord(c->evp[1], st));
-            CK(launch_scan(p, st));
-            CK(cudaEventRecord(c->evp[2], st));
-            CK(launch_expand(p, st));
-            CK(cudaEventRecord(c->evp[3], st));
-            CK(launch_scatter(p, dims, st));
-            CK(cudaEventRecord(c->evp[4], st));
-            launches += 4;
-        } else {
-            CK(cudaEventRecord(c->evp[4], st));
-            // keep the grid and lists; clear the pair count and error word
-            CK(cudaMemsetAsync(&p.ctr->pairs, 0, sizeof(unsigned long long), st));
-            CK(cudaMemsetAsync(&p.ctr->err, 0, sizeof(unsigned int), st));
-        }
-        CK(launch_pairs(p, dims, c->sm_count, st, &c->evp[7]));
-        launches += 3;
-        CK(cudaEventRecord(c->evp[5], st));
-        CK(cudaEventRecord(c->ev1, st));
+        CK(record_pipeline(c, p, dims, grouped, nsc, need_full, st));
+        launches += need_full ? 4 : 0;
+        launches += 3 + (grouped ? 3 : 0);
         CK(cudaMemcpyAsync(c->h_ctr.p, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, st));
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
@@ -380,70 +547,15 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     }
     if (h.err & (kErrEntryOvf | kErrTaskOvf | kErrOutOvf)) return fail(PBIG2_ENOMEM, "capacity retries exhausted");
     c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-    double phase[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < 5; k++) {
-        float x = 0;
-        if (cudaEventElapsedTime(&x, c->evp[k], c->evp[k + 1]) == cudaSuccess) phase[k] = x;
+    int rc = finish_query(c, h, nboxes, ncells, nsc, scenes, grouped, launches, st);
+    if (rc != PBIG2_OK && rc != PBIG2_EINPUT) return rc;
+    // capture this query's pipeline for later batches of the same shape
+    if (G.exec && G.buffers != c->buffers_sig()) c->drop_graph();
+    if (c->use_graph && grouped && !G.exec) {
+        int rg = capture_graph(c, p, d_boxes, nboxes, ncells, nsc, dims, range, split, entry_cap, st);
+        if (rg) return rg;
     }
-    {
-        float x = 0;
-        if (cudaEventElapsedTime(&x, c->evp[4], c->evp[7]) == cudaSuccess) phase[6] = x;
-        if (cudaEventElapsedTime(&x, c->evp[7], c->evp[8]) == cudaSuccess) phase[7] = x;
-        if (cudaEventElapsedTime(&x, c->evp[8], c->evp[5]) == cudaSuccess) phase[8] = x;
-    }
-
-    c->npairs = h.pairs;
-    c->result = c->d_out.as<uint2>();
-    c->scene_pair_off.assign(1, 0);
-    if (group && nsc > 1) {
-        // histogram of pairs per scene on the host from the device copy is too
-        // slow for large outputs; count on the device instead.
-        CK(c->d_scene_pair.ensure((nsc + 1) * 8, false, st));
-        CK(c->d_scene_cursor.ensure((nsc + 1) * 8, false, st));
-        CK(c->d_out2.ensure(std::max<uint64_t>(h.pairs, 1) * 8, false, st));
-        CK(cudaMemsetAsync(c->d_scene_cursor.p, 0, (nsc + 1) * 8, st));
-        Params q = p;
-        q.out_cap = h.pairs;
-        CK(launch_scene_hist(q, c->d_scene_cursor.as<unsigned long long>(), st));
-        std::vector<unsigned long long> hist(nsc + 1);
-        CK(c->h_stage.ensure((nsc + 1) * 8));
-        CK(cudaMemcpyAsync(c->h_stage.p, c->d_scene_cursor.p, (nsc + 1) * 8, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        memcpy(hist.data(), c->h_stage.p, (nsc + 1) * 8);
-        c->scene_pair_off.assign(nsc + 1, 0);
-        for (uint32_t i = 0; i < nsc; i++) c->scene_pair_off[i + 1] = c->scene_pair_off[i] + hist[i];
-        memcpy(c->h_stage.p, c->scene_pair_off.data(), (nsc + 1) * 8);
-        CK(cudaMemcpyAsync(c->d_scene_pair.p, c->h_stage.p, (nsc + 1) * 8, cudaMemcpyHostToDevice, st));
-        CK(cudaMemsetAsync(c->d_scene_cursor.p, 0, (nsc + 1) * 8, st));
-        CK(launch_group_by_scene(q, c->d_scene_pair.as<unsigned long long>(),
-                                 c->d_scene_cursor.as<unsigned long long>(), c->d_out2.as<uint2>(), st));
-        CK(cudaEventRecord(c->ev1, st));
-        CK(cudaStreamSynchronize(st));
-        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-        float x = 0;
-        if (cudaEventElapsedTime(&x, c->evp[5], c->ev1) == cudaSuccess) phase[5] = x;
-        c->result = c->d_out2.as<uint2>();
-        launches += 2;
-    } else {
-        c->scene_pair_off.push_back(h.pairs);
-    }
-    pbig2_stats& s = c->stats;
-    s.boxes = nboxes;
-    s.bad_boxes = h.bad;
-    s.cells = ncells;
-    s.entries = h.entries;
-    s.pair_tests = h.tests;
-    s.pairs = h.pairs;
-    s.cell_shift = scenes.empty() ? 0 : scenes[0].shift;
-    s.scenes = nsc;
-    s.kernels = (uint32_t)launches;
-    s.device_ms = ms;
-    for (int k = 0; k < 9; k++) s.phase_ms[k] = phase[k];
-    if (h.bad) return fail(PBIG2_EINPUT, "%u boxes violate the input contract (error bits 0x%x) and were skipped",
-                           h.bad, h.err);
-    return PBIG2_OK;
+    return rc;
 }
 
 static cudaStream_t pick_stream(pbig2_ctx* c, void* stream) {
@@ -514,10 +626,11 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     if (!c) return PBIG2_OK;
     cudaSetDevice(c->device);
     if (c->own_stream) cudaStreamSynchronize(c->own_stream);
+    c->drop_graph();
     for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_starts, &c->d_entries,
                       &c->d_lists, &c->d_tasks, &c->d_state,
                       &c->d_out, &c->d_out2, &c->d_ctr, &c->d_scenes, &c->d_scene_off, &c->d_scene_pair,
-                      &c->d_scene_cursor})
+                      &c->d_scene_cursor, &c->d_dims})
         b->release();
     c->h_ctr.release();
     c->h_stage.release();
@@ -750,6 +863,16 @@ PBIG2_API int pbig2_result_scene_offsets(pbig2_ctx* c, uint64_t* offsets, uint32
         return fail(PBIG2_EINVAL, "last result has %zu scenes", c->scene_pair_off.size() - 1);
     memcpy(offsets, c->scene_pair_off.data(), (n_scenes + 1) * 8);
     return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_set_option(pbig2_ctx* c, int option, int64_t value) {
+    if (!c) return fail(PBIG2_EINVAL, "bad arguments");
+    if (option == PBIG2_OPT_GRAPH) {
+        c->use_graph = value != 0;
+        if (!c->use_graph) c->drop_graph();
+        return PBIG2_OK;
+    }
+    return fail(PBIG2_EINVAL, "unknown option %d", option);
 }
 
 PBIG2_API int pbig2_get_stats(pbig2_ctx* c, pbig2_stats* s) {

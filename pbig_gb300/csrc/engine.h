@@ -52,7 +52,7 @@ struct pbig2_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evp[9] = {};
     pbig::DevBuf d_boxes, d_counts, d_starts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
-        d_scenes, d_scene_off, d_scene_pair, d_scene_cursor;
+        d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims;
     pbig::HostPinned h_ctr, h_stage;
     bool counts_dirty = false;
     // last result
@@ -62,6 +62,28 @@ struct pbig2_ctx {
     pbig2_stats stats{};
     // capacity hints carried between queries
     uint64_t out_hint = 0;
+    // captured batched pipeline (CUDA graph) and the capacities it serves
+    bool use_graph = true;
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        const uint32_t* boxes = nullptr;
+        int dims = 0;
+        uint32_t range = 0, split = 0;
+        uint64_t nboxes_cap = 0, ncells_cap = 0, nscenes_cap = 0, entry_cap = 0, out_cap = 0;
+        uintptr_t buffers = 0;  // buffers_sig() at capture: any reallocation invalidates the graph
+        int launches = 0;
+    } graph;
+    uintptr_t buffers_sig() const {
+        uintptr_t h = 0;
+        for (const pbig::DevBuf* b : {&d_counts, &d_starts, &d_entries, &d_lists, &d_tasks, &d_state, &d_out, &d_out2,
+                                      &d_ctr, &d_scenes, &d_scene_off, &d_scene_pair, &d_scene_cursor, &d_dims})
+            h = h * 1000003u + (uintptr_t)b->p;
+        return h * 1000003u + (uintptr_t)h_ctr.p;
+    }
+    void drop_graph() {
+        if (graph.exec) cudaGraphExecDestroy(graph.exec);
+        graph = Graph();
+    }
     // autotuner memo: (n, dims, range, mean extent) -> shift
     struct TuneMemo { uint64_t n; int dims; uint32_t range; double ext; uint32_t shift; double est_e; };
     std::vector<TuneMemo> memo;

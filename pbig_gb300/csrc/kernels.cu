@@ -45,6 +45,17 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
     return v;
 }
 
+// kernels take their sizes from device memory when p.dyn is set
+__device__ __forceinline__ Params resolve(const Params& in) {
+    Params p = in;
+    if (p.dyn) {
+        p.nboxes = p.dyn->nboxes;
+        p.ncells = p.dyn->ncells;
+        p.nscenes = p.dyn->nscenes;
+    }
+    return p;
+}
+
 __device__ __forceinline__ uint32_t find_scene(const Params& p, uint64_t gi) {
     if (p.nscenes <= 1) return 0;
     uint32_t lo = 0, hi = p.nscenes;  // last scene s with scene_box_off[s] <= gi
@@ -153,23 +164,29 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
 }
 
 template <int D>
-__global__ void __launch_bounds__(kBoxThreads) k_count(Params p) {
+__global__ void __launch_bounds__(kBoxThreads) k_count(Params pin) {
     __shared__ __align__(16) uint32_t sbox[kBoxThreads * (2 * D + 1)];
-    const uint64_t b0 = (uint64_t)blockIdx.x * kBoxThreads;
-    const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
-    stage_boxes<D>(p, b0, nb, sbox);
-    __syncthreads();
-    enumerate_cells<D, false>(p, sbox, b0, nb);
+    const Params p = resolve(pin);
+    for (uint64_t b0 = (uint64_t)blockIdx.x * kBoxThreads; b0 < p.nboxes; b0 += (uint64_t)gridDim.x * kBoxThreads) {
+        const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
+        stage_boxes<D>(p, b0, nb, sbox);
+        __syncthreads();
+        enumerate_cells<D, false>(p, sbox, b0, nb);
+        __syncthreads();
+    }
 }
 
 template <int D>
-__global__ void __launch_bounds__(kBoxThreads) k_scatter(Params p) {
+__global__ void __launch_bounds__(kBoxThreads) k_scatter(Params pin) {
     __shared__ __align__(16) uint32_t sbox[kBoxThreads * (2 * D + 1)];
-    const uint64_t b0 = (uint64_t)blockIdx.x * kBoxThreads;
-    const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
-    stage_boxes<D>(p, b0, nb, sbox);
-    __syncthreads();
-    enumerate_cells<D, true>(p, sbox, b0, nb);
+    const Params p = resolve(pin);
+    for (uint64_t b0 = (uint64_t)blockIdx.x * kBoxThreads; b0 < p.nboxes; b0 += (uint64_t)gridDim.x * kBoxThreads) {
+        const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
+        stage_boxes<D>(p, b0, nb, sbox);
+        __syncthreads();
+        enumerate_cells<D, true>(p, sbox, b0, nb);
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -203,13 +220,17 @@ __device__ __forceinline__ void st_volatile(unsigned long long* a, unsigned long
     *reinterpret_cast<volatile unsigned long long*>(a) = v;
 }
 
-__global__ void __launch_bounds__(kScanThreads, 5) k_scan(Params p) {
+__global__ void __launch_bounds__(kScanThreads, 5) k_scan(Params pin) {
     __shared__ uint32_t s_tile;
     __shared__ unsigned long long s_warp_tot[8];
     __shared__ unsigned long long s_prefix;
     __shared__ uint32_t s_cls[kNumLists], s_cls_base[kNumLists];
     __shared__ unsigned long long s_tests;
+    const Params p = resolve(pin);
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    const uint64_t tiles = (p.ncells + kScanTile - 1) / kScanTile;
+    // persistent: each block takes tiles in ticket order until none is left
+    for (;;) {
     if (t == 0) {
         s_tile = atomicAdd(&p.ctr->ticket, 1u);
         s_tests = 0;
@@ -217,6 +238,7 @@ __global__ void __launch_bounds__(kScanThreads, 5) k_scan(Params p) {
     if (t < kNumLists) s_cls[t] = 0;
     __syncthreads();
     const uint64_t tile = s_tile;
+    if (tile >= tiles) break;
     const uint64_t c_warp = tile * kScanTile + (uint64_t)warp * 512;  // first cell of this warp
     // load 4 rows x 4 cells per lane
     uint32_t v[16];
@@ -346,6 +368,8 @@ __global__ void __launch_bounds__(kScanThreads, 5) k_scan(Params p) {
         }
         (void)c;
     }
+    __syncthreads();  // shared state is reused by the next tile
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -440,7 +464,7 @@ __device__ __forceinline__ Box load_box(const Params& p, uint32_t raw) {
     Box x;
     x.id = raw & kIdMask;
     x.f = (~(raw >> kIdBits) & 7u) << kMissShift;
-    if (x.id >= p.nboxes) {  // cannot happen with a consistent grid; never read past the boxes
+    if (x.id >= p.nboxes) {  // cannot happen with a consistent grid; never read past the box buffer
         atomicOr(&p.ctr->err, kErrIndex);
         return dummy_box<NARROW>();
     }
@@ -618,9 +642,7 @@ __device__ __forceinline__ void row_unit(const Params& p, const Slots& s, uint32
 
 // ---- small cells ------------------------------------------------------------
 // lane group g (WG lanes) holds cell item*G+g of the class list, lane r its
-// box r; the circular half sweep runs inside the group. A warp loads two
-// items before testing either, so their dependent loads (list record, entry,
-// box) overlap.
+// box r; the circular half sweep runs inside the group.
 template <int D, int WG, bool NARROW>
 __device__ __forceinline__ Box small_fetch(const Params& p, int list, uint64_t nl, uint64_t ci, uint32_t r,
                                            uint32_t& n) {
@@ -665,17 +687,15 @@ __device__ __forceinline__ void small_items(const Params& p, const Slots& s, War
     const uint32_t lane = lane_id(), g = lane / WG, r = lane % WG;
     const uint64_t nl = mn64(p.ctr->n_list[list], p.list_cap[list]);
     const uint64_t nitems = (nl + G - 1) / G;
-    for (uint64_t item = first; item < nitems; item += 2 * stride) {
-        uint32_t n1, n2;
+    for (uint64_t item = first; item < nitems; item += stride) {
+        uint32_t n1;
         const Box a = small_fetch<D, WG, NARROW>(p, list, nl, item * G + g, r, n1);
-        const Box b = small_fetch<D, WG, NARROW>(p, list, nl, (item + stride) * G + g, r, n2);
         small_sweep<D, WG, BIP, NARROW>(p, s, o, a, n1, lane, g, r);
-        small_sweep<D, WG, BIP, NARROW>(p, s, o, b, n2, lane, g, r);
     }
 }
 
 template <int D, bool BIP, bool NARROW>
-__global__ void __launch_bounds__(kPairThreads, 5) k_pairs_small(Params p) {
+__global__ void __launch_bounds__(kPairThreads, 6) k_pairs_small(Params p) {
     __shared__ uint4 s_a[kPairWarps][kSmallSlots], s_b[kPairWarps][kSmallSlots];
     __shared__ uint2 s_out[kPairWarps][kWarpOut];
     const uint32_t warp = threadIdx.x >> 5;
@@ -952,8 +972,10 @@ __device__ __forceinline__ unsigned long long warp_scene_reserve(unsigned long l
     return __shfl_sync(FULL_MASK, base, leader);
 }
 
-__global__ void k_group_by_scene(Params p, const unsigned long long* scene_pair_off,
+__global__ void k_group_by_scene(Params pin, const unsigned long long* scene_pair_off,
                                  unsigned long long* scene_cursor, uint2* dst, unsigned long long n) {
+    const Params p = resolve(pin);
+    n = mn64(p.ctr->pairs, p.out_cap);
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     const unsigned long long n32 = (n + 31) & ~31ull;  // whole warps iterate together
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n32; i += stride) {
@@ -969,7 +991,9 @@ __global__ void k_group_by_scene(Params p, const unsigned long long* scene_pair_
     }
 }
 
-__global__ void k_scene_hist(Params p, unsigned long long* hist, unsigned long long n) {
+__global__ void k_scene_hist(Params pin, unsigned long long* hist, unsigned long long n) {
+    const Params p = resolve(pin);
+    n = mn64(p.ctr->pairs, p.out_cap);
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
     const unsigned long long n32 = (n + 31) & ~31ull;
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n32; i += stride) {
@@ -980,10 +1004,50 @@ __global__ void k_scene_hist(Params p, unsigned long long* hist, unsigned long l
     }
 }
 
+// exclusive scan of the per-scene pair counts: off[s] = sum of hist[< s],
+// off[nscenes] = total; one block, 1024 threads, chunks of 1024 scenes
+__global__ void __launch_bounds__(1024) k_scene_offsets(Params pin, const unsigned long long* hist,
+                                                        unsigned long long* off) {
+    const Params p = resolve(pin);
+    __shared__ unsigned long long s_w[32];
+    __shared__ unsigned long long s_carry;
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    if (t == 0) s_carry = 0;
+    __syncthreads();
+    for (uint32_t c0 = 0; c0 <= p.nscenes; c0 += 1024) {
+        const uint32_t i = c0 + t;
+        const unsigned long long v = i < p.nscenes ? hist[i] : 0ull;
+        unsigned long long x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(FULL_MASK, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_w[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long w = s_w[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long y = __shfl_up_sync(FULL_MASK, w, o);
+                if (lane >= (uint32_t)o) w += y;
+            }
+            s_w[lane] = w;
+        }
+        __syncthreads();
+        const unsigned long long incl = x + (warp ? s_w[warp - 1] : 0ull) + s_carry;
+        if (i <= p.nscenes) off[i] = incl - v;
+        __syncthreads();
+        if (t == 1023) s_carry = incl;
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 static int g_blocks_small = 1, g_blocks_med = 1, g_blocks_block = 1;
+static int g_sm_count = 0;
 
 static size_t med_smem() { return (size_t)kPairWarps * (2 * kMedSlots * sizeof(uint4) + kWarpOut * sizeof(uint2)); }
 
@@ -999,6 +1063,11 @@ static cudaError_t init_variant() {
 
 cudaError_t kernels_init() {
     cudaError_t e;
+    {
+        int dev = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    }
     if ((e = init_variant<2, false, true>()) != cudaSuccess) return e;
     if ((e = init_variant<3, false, true>()) != cudaSuccess) return e;
     if ((e = init_variant<2, true, true>()) != cudaSuccess) return e;
@@ -1018,34 +1087,46 @@ cudaError_t kernels_init() {
 }
 
 cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st) {
-    const unsigned long long n = p.out_cap;
-    if (n == 0) return cudaSuccess;
-    const unsigned long long blocks = mn64((n + 255) / 256, 152ull * 16);
-    k_scene_hist<<<(unsigned)blocks, 256, 0, st>>>(p, hist, n);
+    // the pair count is read on the device
+    k_scene_hist<<<(unsigned)((g_sm_count > 0 ? g_sm_count : 152) * 8), 256, 0, st>>>(p, hist, 0);
     return cudaGetLastError();
 }
 
 uint64_t scan_tiles(uint64_t ncells) { return (ncells + kScanTile - 1) / kScanTile; }
 
+static unsigned box_grid(uint64_t nboxes) {
+    const uint64_t nb = (nboxes + kBoxThreads - 1) / kBoxThreads;
+    const uint64_t cap = (uint64_t)(g_sm_count > 0 ? g_sm_count : 152) * 8;
+    return (unsigned)(nb < cap ? nb : cap);
+}
+
 cudaError_t launch_count(const Params& p, int dims, cudaStream_t st) {
-    const uint64_t nb = (p.nboxes + kBoxThreads - 1) / kBoxThreads;
-    if (nb == 0) return cudaSuccess;
-    if (dims == 2) k_count<2><<<(unsigned)nb, kBoxThreads, 0, st>>>(p);
-    else k_count<3><<<(unsigned)nb, kBoxThreads, 0, st>>>(p);
+    const unsigned g = box_grid(p.nboxes);
+    if (g == 0) return cudaSuccess;
+    if (dims == 2) k_count<2><<<g, kBoxThreads, 0, st>>>(p);
+    else k_count<3><<<g, kBoxThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st) {
-    const uint64_t nb = (p.nboxes + kBoxThreads - 1) / kBoxThreads;
-    if (nb == 0) return cudaSuccess;
-    if (dims == 2) k_scatter<2><<<(unsigned)nb, kBoxThreads, 0, st>>>(p);
-    else k_scatter<3><<<(unsigned)nb, kBoxThreads, 0, st>>>(p);
+    const unsigned g = box_grid(p.nboxes);
+    if (g == 0) return cudaSuccess;
+    if (dims == 2) k_scatter<2><<<g, kBoxThreads, 0, st>>>(p);
+    else k_scatter<3><<<g, kBoxThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scan(const Params& p, cudaStream_t st) {
     const uint64_t tiles = scan_tiles(p.ncells);
-    k_scan<<<(unsigned)tiles, kScanThreads, 0, st>>>(p);
+    const uint64_t cap = (uint64_t)(g_sm_count > 0 ? g_sm_count : 152) * 5;
+    k_scan<<<(unsigned)(tiles < cap ? (tiles ? tiles : 1) : cap), kScanThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scene_offsets(const Params& p, const unsigned long long* hist, unsigned long long* off,
+                                 uint32_t nscenes_cap, cudaStream_t st) {
+    (void)nscenes_cap;
+    k_scene_offsets<<<1, 1024, 0, st>>>(p, hist, off);
     return cudaGetLastError();
 }
 
@@ -1077,11 +1158,9 @@ cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t s
 
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,
                                   unsigned long long* scene_cursor, uint2* dst, cudaStream_t st) {
-    // pair count is read on the host before this launch; p.out_cap carries it
-    const unsigned long long n = p.out_cap;
-    if (n == 0) return cudaSuccess;
-    const unsigned long long blocks = mn64((n + 255) / 256, 152ull * 16);
-    k_group_by_scene<<<(unsigned)blocks, 256, 0, st>>>(p, scene_pair_off, scene_cursor, dst, n);
+    // the pair count is read on the device
+    k_group_by_scene<<<(unsigned)((g_sm_count > 0 ? g_sm_count : 152) * 8), 256, 0, st>>>(p, scene_pair_off,
+                                                                                          scene_cursor, dst, 0);
     return cudaGetLastError();
 }
 

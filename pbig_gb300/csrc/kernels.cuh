@@ -56,6 +56,15 @@ struct Ctr {
     unsigned long long tests;           // sum of n(n-1)/2 over cells
 };
 
+// query sizes read from device memory (graph replays: one captured graph
+// serves every batch up to the capacities it was captured with)
+struct RunDims {
+    unsigned long long nboxes;
+    unsigned long long ncells;
+    unsigned int nscenes;
+    unsigned int pad;
+};
+
 struct Params {
     const uint32_t* boxes;        // RectInfo records, 2*D+1 words each
     uint64_t nboxes;              // boxes over all scenes
@@ -78,13 +87,19 @@ struct Params {
     uint2* out;                   // pairs
     uint64_t out_cap;
     Ctr* ctr;
+    const RunDims* dyn;           // when set, overrides nboxes / ncells / nscenes
 };
 
 // launchers (all asynchronous on `st`); dims is 2 or 3
+// grids: sized from p.nboxes / p.ncells (which must then be upper bounds
+// of the device-side sizes when p.dyn is set)
 cudaError_t launch_count(const Params& p, int dims, cudaStream_t st);
 cudaError_t launch_scan(const Params& p, cudaStream_t st);
 cudaError_t launch_expand(const Params& p, cudaStream_t st);
 cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st);
+// exclusive scan of nscenes+1 per-scene pair counts (one block)
+cudaError_t launch_scene_offsets(const Params& p, const unsigned long long* hist, unsigned long long* off,
+                                 uint32_t nscenes_cap, cudaStream_t st);
 // ev (optional, 2 events) is recorded after the small-cell and after the
 // medium-cell kernel
 cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev = nullptr);

@@ -28,7 +28,7 @@ EXPORTS = [
     "pbig2_bipartite_intersect", "pbig2_batch_intersect", "pbig2_result_pairs", "pbig2_copy_pairs",
     "pbig2_result_scene_offsets", "pbig2_copy_pairs_async", "pbig2_sync", "pbig2_host_alloc",
     "pbig2_host_free", "pbig2_get_stats", "pbig2_tune_shift", "pbig2_self_intersect_noalloc",
-    "pbig2_noalloc_last_error",
+    "pbig2_noalloc_last_error", "pbig2_set_option",
 ]
 
 
@@ -80,6 +80,7 @@ def lib():
         L.pbig2_tune_shift.argtypes = [vp, u64, u32, u32, u64, C.POINTER(u32)]
         L.pbig2_self_intersect_noalloc.argtypes = [vp, u64, u32, u32, u32, vp, u64, C.POINTER(u64), vp]
         L.pbig2_noalloc_last_error.restype = C.c_char_p
+        L.pbig2_set_option.argtypes = [vp, C.c_int, C.c_int64]
         _LIB = L
     return _LIB
 
@@ -230,6 +231,10 @@ class Engine:
 
     def result_count(self) -> int:
         return self.device_pairs()[1]
+
+    def set_graphs(self, on: bool) -> None:
+        """Capture/replay batched queries as CUDA graphs (on by default)."""
+        _check(self._L.pbig2_set_option(self._ctx, 1, int(bool(on))))
 
     def stats(self) -> dict:
         s = Stats()

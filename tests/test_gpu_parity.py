@@ -203,3 +203,34 @@ def test_wide_coordinates(engine, name):
     assert rng_w > (1 << 29)
     assert engine.self_intersect(wide, rng_w) == len(want)
     assert np.array_equal(canon(engine.pairs()), want)
+
+
+def test_batched_graph_replay_matches_eager(engine):
+    """Batched queries replay a captured CUDA graph once the first query of a
+    shape ran; the replay (same batch, then a smaller batch in the same
+    buffer) must give the eager results."""
+    import torch
+    parts, offs = _scenes(40, 7, 256, 30000)
+    allb = np.ascontiguousarray(np.concatenate(parts))
+    dev = to_device(allb)
+    results = []
+    for graphs in (False, True):
+        engine.set_graphs(graphs)
+        for rep in range(3):  # eager, capture, replay
+            total = engine.batch_intersect(dev, offs, gen.RANGE)
+            so = engine.scene_offsets()
+            res = engine.pairs()
+            results.append([canon(res[int(so[i]):int(so[i + 1])]) for i in range(len(parts))])
+    for r in results[1:]:
+        for a, b in zip(results[0], r):
+            assert np.array_equal(a, b)
+    # a smaller batch (first 25 scenes) in the same device buffer replays the graph too
+    engine.set_graphs(True)
+    sub = dev[: int(offs[25])]
+    offs25 = offs[:26].copy()
+    assert engine.batch_intersect(sub, offs25, gen.RANGE) == sum(len(x) for x in results[0][:25])
+    so = engine.scene_offsets()
+    res = engine.pairs()
+    for i in range(25):
+        assert np.array_equal(canon(res[int(so[i]):int(so[i + 1])]), results[0][i])
+    engine.set_graphs(True)
