@@ -256,11 +256,17 @@ static int ensure_query_buffers(pbig2_ctx* c, Params& p, uint64_t entry_cap, uin
 // the launches of one pipeline pass (also what a graph captures): counters
 // and scan state reset, count, scan, expand, scatter, the three pair
 // kernels and, for batches, grouping of the pairs by scene
+static int g_record_line = 0;  // line of the call that failed in record_pipeline
+
 static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool grouped, uint32_t nsc,
                                    bool full, cudaStream_t st) {
     cudaError_t e;
+    (void)cudaGetLastError();  // launch checks below must not see older, unrelated errors
 #define R(x)                          \
-    if ((e = (x)) != cudaSuccess) return e;
+    if ((e = (x)) != cudaSuccess) {   \
+        g_record_line = __LINE__;     \
+        return e;                     \
+    }
     if (full) {
         R(cudaMemsetAsync(p.ctr, 0, sizeof(Ctr), st));
         R(cudaMemsetAsync(p.tile_state, 0, scan_tiles(p.ncells) * 8, st));
@@ -335,6 +341,7 @@ static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t nc
     s.kernels = (uint32_t)launches;
     s.device_ms = ms;
     for (int k = 0; k < 9; k++) s.phase_ms[k] = phase[k];
+    (void)cudaGetLastError();  // a timing query on an unrecorded event is not an error of the query
     if (h.bad) return fail(PBIG2_EINPUT, "%u boxes violate the input contract (error bits 0x%x) and were skipped",
                            h.bad, h.err);
     return PBIG2_OK;
@@ -448,6 +455,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     Ctr h{};
     int launches = 0;
     if (graph_fits) {
+        CK(cudaEventRecord(c->ev0, st));
         CK(cudaGraphLaunch(G.exec, st));
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
@@ -506,7 +514,11 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         int rc = ensure_query_buffers(c, p, entry_cap, out_cap, task_cap, nsc, grouped, st);
         if (rc) return rc;
         if (attempt == 0) CK(cudaEventRecord(c->ev0, st));
-        CK(record_pipeline(c, p, dims, grouped, nsc, need_full, st));
+        {
+            const cudaError_t re = record_pipeline(c, p, dims, grouped, nsc, need_full, st);
+            if (re != cudaSuccess)
+                return fail(PBIG2_ECUDA, "pipeline launch (engine.cu:%d): %s", g_record_line, cudaGetErrorString(re));
+        }
         launches += need_full ? 4 : 0;
         launches += 3 + (grouped ? 3 : 0);
         CK(cudaMemcpyAsync(c->h_ctr.p, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, st));
