@@ -1138,9 +1138,9 @@ cudaError_t launch_expand(const Params& p, cudaStream_t st) {
 template <int D, bool B, bool N>
 static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st, cudaEvent_t* ev) {
     k_pairs_small<D, B, N><<<sm_count * g_blocks_small, kPairThreads, 0, st>>>(p);
-    if (ev) cudaEventRecord(ev[0], st);
+    if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
     k_pairs_med<D, B, N><<<sm_count * g_blocks_med, kPairThreads, med_smem(), st>>>(p);
-    if (ev) cudaEventRecord(ev[1], st);
+    if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
     k_pairs_block<D, B, N><<<sm_count * g_blocks_block, kPairThreads, sizeof(BlockSmem), st>>>(p);
     return cudaGetLastError();
 }
