@@ -262,6 +262,10 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
                                    bool full, cudaStream_t st) {
     cudaError_t e;
     (void)cudaGetLastError();  // launch checks below must not see older, unrelated errors
+    // inside a stream capture an event record must be an external node to be timed
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if ((e = cudaStreamIsCapturing(st, &cap)) != cudaSuccess) return e;
+    const unsigned evf = cap == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
 #define R(x)                          \
     if ((e = (x)) != cudaSuccess) {   \
         g_record_line = __LINE__;     \
@@ -270,23 +274,23 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
     if (full) {
         R(cudaMemsetAsync(p.ctr, 0, sizeof(Ctr), st));
         R(cudaMemsetAsync(p.tile_state, 0, scan_tiles(p.ncells) * 8, st));
-        R(cudaEventRecordWithFlags(c->evp[0], st, cudaEventRecordExternal));
+        R(cudaEventRecordWithFlags(c->evp[0], st, evf));
         R(launch_count(p, dims, st));
-        R(cudaEventRecordWithFlags(c->evp[1], st, cudaEventRecordExternal));
+        R(cudaEventRecordWithFlags(c->evp[1], st, evf));
         R(launch_scan(p, st));
-        R(cudaEventRecordWithFlags(c->evp[2], st, cudaEventRecordExternal));
+        R(cudaEventRecordWithFlags(c->evp[2], st, evf));
         R(launch_expand(p, st));
-        R(cudaEventRecordWithFlags(c->evp[3], st, cudaEventRecordExternal));
+        R(cudaEventRecordWithFlags(c->evp[3], st, evf));
         R(launch_scatter(p, dims, st));
-        R(cudaEventRecordWithFlags(c->evp[4], st, cudaEventRecordExternal));
+        R(cudaEventRecordWithFlags(c->evp[4], st, evf));
     } else {
         // keep the grid and lists; clear the pair count and error word
         R(cudaMemsetAsync(&p.ctr->pairs, 0, sizeof(unsigned long long), st));
         R(cudaMemsetAsync(&p.ctr->err, 0, sizeof(unsigned int), st));
-        R(cudaEventRecordWithFlags(c->evp[4], st, cudaEventRecordExternal));
+        R(cudaEventRecordWithFlags(c->evp[4], st, evf));
     }
-    R(launch_pairs(p, dims, c->sm_count, st, &c->evp[7]));  // records evp[7], evp[8] (external)
-    R(cudaEventRecordWithFlags(c->evp[5], st, cudaEventRecordExternal));
+    R(launch_pairs(p, dims, c->sm_count, st, &c->evp[7], evf));  // records evp[7], evp[8]
+    R(cudaEventRecordWithFlags(c->evp[5], st, evf));
     if (grouped) {
         unsigned long long* hist = c->d_scene_cursor.as<unsigned long long>();
         unsigned long long* offs = c->d_scene_pair.as<unsigned long long>();
@@ -296,7 +300,7 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
         R(cudaMemsetAsync(hist, 0, (nsc + 1) * 8, st));
         R(launch_group_by_scene(p, offs, hist, c->d_out2.as<uint2>(), st));
     }
-    R(cudaEventRecordWithFlags(c->ev1, st, cudaEventRecordExternal));
+    R(cudaEventRecordWithFlags(c->ev1, st, evf));
 #undef R
     return cudaSuccess;
 }

@@ -1136,24 +1136,24 @@ cudaError_t launch_expand(const Params& p, cudaStream_t st) {
 }
 
 template <int D, bool B, bool N>
-static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st, cudaEvent_t* ev) {
+static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st, cudaEvent_t* ev, unsigned evf) {
     k_pairs_small<D, B, N><<<sm_count * g_blocks_small, kPairThreads, 0, st>>>(p);
-    if (ev) cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
+    if (ev) cudaEventRecordWithFlags(ev[0], st, evf);
     k_pairs_med<D, B, N><<<sm_count * g_blocks_med, kPairThreads, med_smem(), st>>>(p);
-    if (ev) cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
+    if (ev) cudaEventRecordWithFlags(ev[1], st, evf);
     k_pairs_block<D, B, N><<<sm_count * g_blocks_block, kPairThreads, sizeof(BlockSmem), st>>>(p);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev) {
+cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev, unsigned evf) {
     const bool bip = p.split != kNoSplit;
     const bool narrow = p.max_range <= (1u << kMissShift);
     if (narrow) {
-        if (dims == 2) return bip ? launch_pairs_t<2, true, true>(p, sm_count, st, ev) : launch_pairs_t<2, false, true>(p, sm_count, st, ev);
-        return bip ? launch_pairs_t<3, true, true>(p, sm_count, st, ev) : launch_pairs_t<3, false, true>(p, sm_count, st, ev);
+        if (dims == 2) return bip ? launch_pairs_t<2, true, true>(p, sm_count, st, ev, evf) : launch_pairs_t<2, false, true>(p, sm_count, st, ev, evf);
+        return bip ? launch_pairs_t<3, true, true>(p, sm_count, st, ev, evf) : launch_pairs_t<3, false, true>(p, sm_count, st, ev, evf);
     }
-    if (dims == 2) return bip ? launch_pairs_t<2, true, false>(p, sm_count, st, ev) : launch_pairs_t<2, false, false>(p, sm_count, st, ev);
-    return bip ? launch_pairs_t<3, true, false>(p, sm_count, st, ev) : launch_pairs_t<3, false, false>(p, sm_count, st, ev);
+    if (dims == 2) return bip ? launch_pairs_t<2, true, false>(p, sm_count, st, ev, evf) : launch_pairs_t<2, false, false>(p, sm_count, st, ev, evf);
+    return bip ? launch_pairs_t<3, true, false>(p, sm_count, st, ev, evf) : launch_pairs_t<3, false, false>(p, sm_count, st, ev, evf);
 }
 
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,

@@ -102,7 +102,8 @@ cudaError_t launch_scene_offsets(const Params& p, const unsigned long long* hist
                                  uint32_t nscenes_cap, cudaStream_t st);
 // ev (optional, 2 events) is recorded after the small-cell and after the
 // medium-cell kernel
-cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev = nullptr);
+cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev = nullptr,
+                         unsigned ev_flags = cudaEventRecordDefault);
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,
                                   unsigned long long* scene_cursor, uint2* dst, cudaStream_t st);
 cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st);
