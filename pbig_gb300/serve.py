@@ -87,8 +87,10 @@ class Server:
         self.engines = [Engine(device) for _ in range(slots)]
         for e in self.engines:
             e.set_graphs(False)  # every batch has a new layout
-        # each slot orders its uploads and its batch on its own stream
+        # each slot orders its uploads and its batch on its own stream, and
+        # downloads pairs into its own page-locked buffer
         self.streams = [torch.cuda.Stream(device=device) for _ in range(slots)]
+        self.pinned = [torch.empty((1 << 20, 2), dtype=torch.int32).pin_memory() for _ in range(slots)]
         self.free_slots = list(range(slots))
         self.batches = 0
         self.t0 = time.perf_counter()
@@ -182,10 +184,15 @@ class Server:
                 offs[i + 1] = offs[i] + sc.host.shape[0]
             cat = torch.cat([sc.dev for sc in scenes]) if len(scenes) > 1 else scenes[0].dev
             shifts = np.array([sc.shift for sc in scenes], dtype=np.uint32)
-            eng.batch_intersect(cat, offs, gen.RANGE, cell_shifts=shifts, stream=stream)
-        so = eng.scene_offsets()
-        if self.keep_pairs:
-            allp = eng.pairs()
+            total = eng.batch_intersect(cat, offs, gen.RANGE, cell_shifts=shifts, stream=stream)
+            so = eng.scene_offsets()
+            if self.keep_pairs:
+                if self.pinned[slot].shape[0] < total:
+                    self.pinned[slot] = torch.empty((int(total * 1.25) + 1024, 2), dtype=torch.int32).pin_memory()
+                buf = self.pinned[slot][:total]
+                eng.pairs_into(buf, stream=stream)
+                eng.sync(stream)
+                allp = buf.numpy().view(np.uint32).copy()
         t_done = self.now()
         for i, r in enumerate(batch):
             r.npairs = int(so[i + 1] - so[i])
@@ -211,18 +218,16 @@ class Server:
         for r, sc in zip(batch, scenes):
             r.nboxes = sc.host.shape[0]
             if sc.shift < 0:  # first query of the scene: tune its cell size once
-                sc.shift = tune_shift(sc.host, gen.RANGE, 512)
+                sc.shift = tune_shift(sc.host, gen.RANGE, 256)
             if r.kind == "update":  # move a fraction of the boxes (host master copy)
-                n = sc.host.shape[0]
-                k = max(1, int(round(r.move_frac * n)))
-                rng = np.random.default_rng(r.move_seed)
-                idx = np.sort(rng.choice(n, size=k, replace=False)).astype(np.uint32)
+                idx = move_indices(sc.host.shape[0], r.move_frac, r.move_seed)
                 gen.move3d(sc.host, idx, r.move_seed, r.move_sigma)
             if sc.dev is None:  # not on the device (new or dropped): upload it whole
-                sc.dev = torch.from_numpy(sc.host.view(np.int32)).to(dev)
+                sc.dev = torch.from_numpy(sc.host.view(np.int32)).to(dev, non_blocking=True)
             elif r.kind == "update":  # upload the moved rows only
-                ti = torch.from_numpy(idx.astype(np.int64)).to(dev)
-                sc.dev[ti] = torch.from_numpy(sc.host[idx].view(np.int32)).to(dev)
+                ti = torch.from_numpy(idx.astype(np.int64)).to(dev, non_blocking=True)
+                rows = torch.from_numpy(sc.host[idx].view(np.int32)).pin_memory()
+                sc.dev[ti] = rows.to(dev, non_blocking=True)
             if self.keep_snapshots:
                 r.snapshot = sc.host.copy()
 
@@ -255,8 +260,24 @@ class Server:
             e.close()
 
 
+def move_indices(n: int, frac: float, seed: int) -> np.ndarray:
+    """round(frac * n) (at least 1) distinct box indices, seeded, sorted."""
+    k = min(n, max(1, int(round(frac * n))))
+    rng = np.random.default_rng(seed)
+    idx = np.unique(rng.integers(0, n, size=k + k // 4 + 8))
+    while idx.shape[0] < k:
+        idx = np.unique(np.concatenate([idx, rng.integers(0, n, size=k)]))
+    return np.sort(rng.permutation(idx)[:k]).astype(np.uint32)
+
+
+def pinned_boxes(n: int) -> np.ndarray:
+    """A page-locked [n,7] uint32 host array (fast host<->device copies)."""
+    import torch
+    return torch.empty((n, 7), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+
+
 def make_requests(duration: float, rate: float = 2000.0, seed: int = 0, lo: int = 1024, hi: int = 1 << 20,
-                  update_frac: float = 0.3, move_frac: float = 0.01) -> list[Request]:
+                  update_frac: float = 0.3, move_frac: float = 0.01, pinned: bool = True) -> list[Request]:
     """Seeded request stream: Poisson arrivals, `update_frac` of them updates
     of an earlier scene (uniform over the scenes queried before), the rest
     queries of new scenes with log-uniform sizes in [lo, hi] (the batched
@@ -274,7 +295,8 @@ def make_requests(duration: float, rate: float = 2000.0, seed: int = 0, lo: int 
             n = int(gen.scene_sizes(1, seed * 7919 + i, lo, hi)[0])
             sid = len(scene_ids)
             scene_ids.append(sid)
-            reqs.append(Request(i, t, sid, "query", boxes=gen.scene3d(n, seed=seed * 1000003 + i)))
+            out = pinned_boxes(n) if pinned else None
+            reqs.append(Request(i, t, sid, "query", boxes=gen.scene3d(n, seed=seed * 1000003 + i, out=out)))
         i += 1
     return reqs
 
