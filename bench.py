@@ -431,6 +431,7 @@ def run_serving(args, rank, local, ws):
         "batches": srv.batches, "mean_batch_requests": len(reqs) / max(1, srv.batches),
         "gpu_slot_busy_fraction": srv.busy_time / max(1e-9, s["span_s"]) / len(srv.engines),
         "evictions": srv.evictions, "refused": srv.refused,
+        "host_ms_per_batch": {k: v * 1e3 / max(1, srv.batches) for k, v in srv.phase_s.items()},
         "clocks": clk.summary(),
     }
     srv.close()

@@ -97,6 +97,7 @@ class Server:
         self.busy_time = 0.0
         self.evictions = 0
         self.refused = 0
+        self.phase_s = collections.defaultdict(float)  # host seconds per batch phase (summed)
 
     # ---- request intake -------------------------------------------------
     def now(self) -> float:
@@ -177,15 +178,19 @@ class Server:
         scenes = [self.scenes[r.scene] for r in batch]
         dev = f"cuda:{self.device}"
         stream = self.streams[slot]
+        tp = [time.perf_counter()]
         with torch.cuda.stream(stream):
             self._prepare(batch, scenes, dev)
+            tp.append(time.perf_counter())
             offs = np.zeros(len(batch) + 1, dtype=np.uint64)
             for i, sc in enumerate(scenes):
                 offs[i + 1] = offs[i] + sc.host.shape[0]
             cat = torch.cat([sc.dev for sc in scenes]) if len(scenes) > 1 else scenes[0].dev
             shifts = np.array([sc.shift for sc in scenes], dtype=np.uint32)
+            tp.append(time.perf_counter())
             total = eng.batch_intersect(cat, offs, gen.RANGE, cell_shifts=shifts, stream=stream)
             so = eng.scene_offsets()
+            tp.append(time.perf_counter())
             if self.keep_pairs:
                 if self.pinned[slot].shape[0] < total:
                     self.pinned[slot] = torch.empty((int(total * 1.25) + 1024, 2), dtype=torch.int32).pin_memory()
@@ -193,6 +198,7 @@ class Server:
                 eng.pairs_into(buf, stream=stream)
                 eng.sync(stream)
                 allp = buf.numpy().view(np.uint32).copy()
+        tp.append(time.perf_counter())
         t_done = self.now()
         for i, r in enumerate(batch):
             r.npairs = int(so[i + 1] - so[i])
@@ -201,6 +207,9 @@ class Server:
             r.done = t_done
             r.batch = self.batches
         with self.lock:
+            for k, name in enumerate(("prepare", "concat", "query", "download")):
+                if k + 1 < len(tp):
+                    self.phase_s[name] += tp[k + 1] - tp[k]
             self.batches += 1
             self.busy_time += t_done - t_start
             for sc in scenes:
