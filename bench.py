@@ -58,7 +58,28 @@ def workload(name: str):
         return gen.clustered3d(1048576, seed=0), gen.RANGE, "3D self-intersection, 1,048,576 boxes, 64-Gaussian mixture (sigma 0.02), lognormal sides (median 0.002, log-sigma 0.5), seed 0 (profiling size)"
     if name == "plain2d":
         return gen.uniform2d(65536, seed=0), gen.RANGE, "2D self-intersection, 65,536 boxes, uniform corners, sides U[0.001,0.005], seed 0"
+    if name == "bipartite4m":
+        return ((gen.mixed3d(2097152, seed=0), gen.mixed3d(2097152, seed=1)), gen.RANGE,
+                "3D bipartite red/blue, 2,097,152 red (seed 0) vs 2,097,152 blue (seed 1) boxes, uniform centres, "
+                "sides U[0.001,0.004], 1% large with sides U[0.02,0.1]; red-blue pairs only")
     raise SystemExit(f"unknown workload {name}")
+
+
+def nboxes(boxes) -> int:
+    return sum(len(b) for b in boxes) if isinstance(boxes, tuple) else len(boxes)
+
+
+def cpu_sample(boxes, m: int):
+    """The first m boxes of a self-intersection workload; for a red/blue
+    workload the union of the first m/2 red and m/2 blue boxes (blue rids
+    renumbered after red): the reference has no red/blue mode, so its CPU
+    path self-intersects the union."""
+    if not isinstance(boxes, tuple):
+        return boxes[:m]
+    red, blue = boxes[0][:m // 2], boxes[1][:m - m // 2]
+    u = np.concatenate([red, blue])
+    u[len(red):, -1] += len(red)
+    return np.ascontiguousarray(u)
 
 
 class ClockSampler:
@@ -128,25 +149,27 @@ def cpu_baseline(boxes, range_, budget_s: float, threads: int):
     heuristic, all host threads) on the first n' boxes, n' sized so that one
     run takes about budget_s seconds."""
     from oracle import oracle as O
-    n = len(boxes)
+    n = nboxes(boxes)
     frac = 1 / 64
     m = max(1024, int(n * frac))
     t0 = time.perf_counter()
-    O.grid_pairs(boxes[:m], range_, count_only=True, threads=threads)
+    O.grid_pairs(cpu_sample(boxes, m), range_, count_only=True, threads=threads)
     dt = time.perf_counter() - t0
     # the reference heuristic keeps the work per box roughly proportional to
     # the density, so time grows ~ n'^2 at fixed domain: scale conservatively
     while m < n and dt < budget_s / 4:
         m = min(n, m * 2)
         t0 = time.perf_counter()
-        _, st = O.grid_pairs(boxes[:m], range_, count_only=True, threads=threads)
+        _, st = O.grid_pairs(cpu_sample(boxes, m), range_, count_only=True, threads=threads)
         dt = time.perf_counter() - t0
-    _, st = O.grid_pairs(boxes[:m], range_, count_only=True, threads=threads)
+    smp = cpu_sample(boxes, m)
+    _, st = O.grid_pairs(smp, range_, count_only=True, threads=threads)
     t0 = time.perf_counter()
-    _, st = O.grid_pairs(boxes[:m], range_, count_only=True, threads=threads)
+    _, st = O.grid_pairs(smp, range_, count_only=True, threads=threads)
     dt = time.perf_counter() - t0
+    what = "union of the first m/2 red and blue boxes, self-intersected" if isinstance(boxes, tuple) else "first boxes"
     return {"value": m / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {m} of {n} boxes (same generator), oracle grid pipeline with the reference cell-size heuristic (cs={st['cs']}), {st['pairs']} pairs, {dt:.2f} s",
+            "sample": f"{m} of {n} boxes ({what}; same generator), oracle grid pipeline with the reference cell-size heuristic (cs={st['cs']}), {st['pairs']} pairs, {dt:.2f} s",
             "pairs_per_s": st["pairs"] / dt}
 
 
@@ -192,15 +215,15 @@ def run_reference(args, rank, ws):
     threads = os.cpu_count() or 1
     total_budget = 150.0
     per_step = total_budget / max(1, args.steps + args.warmup)
-    n = len(boxes)
+    n = nboxes(boxes)
     m = max(1024, n // 64)
     while m < n:
         t0 = time.perf_counter()
-        O.grid_pairs(boxes[:m], rng, count_only=True, threads=threads)
+        O.grid_pairs(cpu_sample(boxes, m), rng, count_only=True, threads=threads)
         if time.perf_counter() - t0 > per_step / 3:
             break
         m = min(n, m * 2)
-    sample = boxes[:m]
+    sample = cpu_sample(boxes, m)
     for _ in range(args.warmup):
         O.grid_pairs(sample, rng, count_only=True, threads=threads)
     ts = []
@@ -216,7 +239,7 @@ def run_reference(args, rank, ws):
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": desc, "sample_boxes": m, "parallelism": "cpu threads"},
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"first {m} of {n} boxes per step; oracle restatement of the reference grid pipeline with its cell-size heuristic (cs={st['cs']}); {st['pairs']} pairs per step"},
+                             "sample": f"{m} of {n} boxes per step ({'red/blue union' if isinstance(boxes, tuple) else 'first boxes'}); oracle restatement of the reference grid pipeline with its cell-size heuristic (cs={st['cs']}); {st['pairs']} pairs per step"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "pairs_per_s": st["pairs"] / t}
     print(json.dumps(line), flush=True)
@@ -228,15 +251,21 @@ def run_gb300(args, rank, local, ws):
 
     torch.cuda.set_device(local)
     boxes, rng, desc = workload(args.workload)
-    n = len(boxes)
-    dev = torch.from_numpy(boxes.view(np.int32)).to(f"cuda:{local}")
-    host = torch.from_numpy(boxes.view(np.int32)).pin_memory()
+    n = nboxes(boxes)
+    parts = boxes if isinstance(boxes, tuple) else (boxes,)
+    dev = [torch.from_numpy(b.view(np.int32)).to(f"cuda:{local}") for b in parts]
+    host = [torch.from_numpy(b.view(np.int32)).pin_memory() for b in parts]
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")  # > L2 (129 MB)
     eng = Engine(local)
 
+    def query(src):
+        if len(src) == 2:
+            return eng.bipartite_intersect(src[0], src[1], rng, stream=stream)
+        return eng.self_intersect(src[0], rng, stream=stream)
+
     for _ in range(args.warmup):
-        eng.self_intersect(dev, rng, stream=stream)
+        query(dev)
         torch.cuda.synchronize()
     P = eng.result_count()
     out_host = torch.empty((P, 2), dtype=torch.int32).pin_memory()
@@ -252,7 +281,7 @@ def run_gb300(args, rank, local, ws):
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            np_ = eng.self_intersect(dev, rng, stream=stream)
+            np_ = query(dev)
             b.record(stream)
             b.synchronize()
             step_ms.append(a.elapsed_time(b))
@@ -272,7 +301,7 @@ def run_gb300(args, rank, local, ws):
     for i in range(max(2, args.steps // 2) + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        eng.self_intersect(host, rng, stream=stream)
+        query(host)
         eng.pairs_into(out_host, stream=stream)
         eng.sync(stream)
         t1 = time.perf_counter()
@@ -283,7 +312,10 @@ def run_gb300(args, rank, local, ws):
            "d2h_bytes_per_step": P * 8, "ms_per_step": e2e_step * 1e3, "pairs_per_s": P * ws / e2e_step}
     # parity spot check of the e2e copy (canonical pairs)
     got = out_host.numpy().view(np.uint32)
-    assert (got[:, 0] < got[:, 1]).all()
+    if len(parts) == 1:
+        assert (got[:, 0] < got[:, 1]).all()
+    else:
+        assert (got[:, 0] < len(parts[0])).all() and (got[:, 1] < len(parts[1])).all()
 
     # roofline of the dominant kernel
     peak, peak_kind = peaks()
@@ -412,7 +444,9 @@ def run_serving(args, rank, local, ws):
     srv.serve(len(warm))
     th.join()
     srv.close()
-    srv = serve.Server(device=local, budget_bytes=40 << 30)
+    # pairs are delivered into each slot's page-locked host buffer (the
+    # device->host copy is timed; no second host copy)
+    srv = serve.Server(device=local, budget_bytes=40 << 30, copy_pairs=False)
     with ClockSampler(local) as clk:
         th = serve.feed(srv, reqs)
         srv.serve(len(reqs))

@@ -18,6 +18,7 @@
 #include <stdint.h>
 #include <string.h>
 #include <pthread.h>
+#include <stdlib.h>
 
 #define QSCALE 16777216.0 /* 2^24 */
 #define QMAX 16777215u
@@ -274,16 +275,78 @@ double pbig_gen_normal(uint64_t seed, uint64_t stream, uint64_t idx) {
     return normal(seed, stream, idx);
 }
 
+static uint64_t gcd64(uint64_t a, uint64_t b) {
+    while (b) { uint64_t t = a % b; a = b; b = t; }
+    return a;
+}
+
+static int cmp_u32(const void* a, const void* b) {
+    uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
+    return x < y ? -1 : x > y;
+}
+
+/* k distinct indices in [0, n), sorted: the arithmetic progression
+ * start + j*step (mod n), j < k, with start and step drawn from the seed and
+ * step coprime to n (so the k values are distinct). */
+int pbig_gen_pick(uint64_t n, uint64_t k, uint64_t seed, uint32_t* out) {
+    if (n == 0 || k > n) return -1;
+    uint64_t start = rng_u64(seed, S_PICK, 0) % n;
+    uint64_t step = n > 1 ? 1 + rng_u64(seed, S_PICK, 1) % (n - 1) : 1;
+    for (uint64_t t = 2; gcd64(step, n) != 1; t++) step = 1 + rng_u64(seed, S_PICK, t) % (n - 1);
+    uint64_t x = start;
+    for (uint64_t j = 0; j < k; j++) {
+        out[j] = (uint32_t)x;
+        x += step;
+        if (x >= n) x -= n;
+    }
+    qsort(out, k, sizeof(uint32_t), cmp_u32);
+    return 0;
+}
+
 /* Move boxes of a resident 3-D scene: for each listed box, shift it by
  * N(0, sigma) per axis (in [0,1) units), keeping its extent, and
  * re-quantise. idx[] are box indices, k of them. */
+/* Division-free variants of the log and cos2pi series above for the update
+ * stream (same expansions; the reciprocal coefficients are compile-time
+ * constants, so results differ from pbig_gen_log/cos2pi by rounding only). */
+static const double INV_ODD[14] = {1.0, 1.0 / 3, 1.0 / 5, 1.0 / 7, 1.0 / 9, 1.0 / 11, 1.0 / 13,
+                                   1.0 / 15, 1.0 / 17, 1.0 / 19, 1.0 / 21, 1.0 / 23, 1.0 / 25, 1.0 / 27};
+static const double COS_C[18] = {1.0 / 2, 1.0 / 12, 1.0 / 30, 1.0 / 56, 1.0 / 90, 1.0 / 132,
+                                 1.0 / 182, 1.0 / 240, 1.0 / 306, 1.0 / 380, 1.0 / 462, 1.0 / 552,
+                                 1.0 / 650, 1.0 / 756, 1.0 / 870, 1.0 / 992, 1.0 / 1122, 1.0 / 1260};
+
+static double log_nodiv(double x) {
+    int e;
+    double m = frexp(x, &e);
+    if (m < 0.70710678118654752440) { m *= 2.0; e -= 1; }
+    double z = (m - 1.0) / (m + 1.0);
+    double z2 = z * z, acc = 0.0;
+    for (int k = 13; k >= 0; k--) acc = acc * z2 + INV_ODD[k];
+    return 2.0 * z * acc + (double)e * LN2;
+}
+
+static double cos2pi_nodiv(double u) {
+    double t = u - floor(u + 0.5);
+    double a = TWO_PI * t;
+    double a2 = a * a, acc = 1.0;
+    /* cos a = 1 - a2/(1*2) (1 - a2/(3*4) (1 - ...)) */
+    for (int k = 17; k >= 0; k--) acc = 1.0 - a2 * COS_C[k] * acc;
+    return acc;
+}
+
+static inline double normal_nodiv(uint64_t seed, uint64_t stream, uint64_t idx) {
+    double u1 = 1.0 - u01(seed, stream, 2 * idx);
+    double u2 = u01(seed, stream, 2 * idx + 1);
+    return sqrt(-2.0 * log_nodiv(u1)) * cos2pi_nodiv(u2);
+}
+
 int pbig_gen_move3d(uint32_t* boxes, const uint32_t* idx, uint64_t k, uint64_t seed,
                     double sigma) {
     for (uint64_t t = 0; t < k; t++) {
         uint32_t* b = boxes + (uint64_t)idx[t] * 7;
         double lo[3], hi[3];
         for (int d = 0; d < 3; d++) {
-            double dx = sigma * normal(seed, S_MOVE, 3 * t + d);
+            double dx = sigma * normal_nodiv(seed, S_MOVE, 3 * t + d);
             double a = (double)b[2 * d] / QSCALE, c = (double)b[2 * d + 1] / QSCALE;
             lo[d] = a + dx;
             hi[d] = c + dx;
@@ -292,3 +355,6 @@ int pbig_gen_move3d(uint32_t* boxes, const uint32_t* idx, uint64_t k, uint64_t s
     }
     return 0;
 }
+
+double pbig_gen_log_nodiv(double x) { return log_nodiv(x); }
+double pbig_gen_cos2pi_nodiv(double u) { return cos2pi_nodiv(u); }

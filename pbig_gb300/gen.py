@@ -35,7 +35,8 @@ def _lib():
         L.pbig_gen_normal.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
         L.pbig_gen_normal.restype = C.c_double
         L.pbig_gen_move3d.argtypes = [u32p, u32p, C.c_uint64, C.c_uint64, C.c_double]
-        for f in ("log", "exp", "cos2pi"):
+        L.pbig_gen_pick.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, u32p]
+        for f in ("log", "exp", "cos2pi", "log_nodiv", "cos2pi_nodiv"):
             fn = getattr(L, "pbig_gen_" + f)
             fn.argtypes = [C.c_double]
             fn.restype = C.c_double
@@ -113,6 +114,15 @@ def move3d(boxes: np.ndarray, idx: np.ndarray, seed: int, sigma: float = 0.001) 
     assert boxes.dtype == np.uint32 and boxes.shape[1] == 7 and boxes.flags.c_contiguous
     idx = np.ascontiguousarray(idx, dtype=np.uint32)
     _lib().pbig_gen_move3d(_p(boxes), _p(idx), idx.shape[0], seed, sigma)
+
+
+def pick(n: int, k: int, seed: int) -> np.ndarray:
+    """k distinct sorted indices in [0, n) (seeded arithmetic progression with
+    a step coprime to n)."""
+    out = np.empty(k, dtype=np.uint32)
+    if _lib().pbig_gen_pick(n, k, seed, _p(out)) != 0:
+        raise ValueError("need 0 < k <= n")
+    return out
 
 
 def digest(boxes: np.ndarray) -> str:

@@ -70,7 +70,8 @@ class Scene:
 
 class Server:
     def __init__(self, device: int = 0, budget_bytes: int = 40 << 30, slots: int = 2,
-                 max_batch_boxes: int = 64 << 20, keep_pairs: bool = True, keep_snapshots: bool = False):
+                 max_batch_boxes: int = 64 << 20, keep_pairs: bool = True, keep_snapshots: bool = False,
+                 copy_pairs: bool = True):
         import torch
         self.torch = torch
         self.device = device
@@ -78,6 +79,7 @@ class Server:
         self.max_batch_boxes = max_batch_boxes
         self.keep_pairs = keep_pairs
         self.keep_snapshots = keep_snapshots
+        self.copy_pairs = copy_pairs
         self.scenes: "collections.OrderedDict[int, Scene]" = collections.OrderedDict()
         self.resident_bytes = 0
         self.inflight_bytes = 0
@@ -91,6 +93,7 @@ class Server:
         # downloads pairs into its own page-locked buffer
         self.streams = [torch.cuda.Stream(device=device) for _ in range(slots)]
         self.pinned = [torch.empty((1 << 20, 2), dtype=torch.int32).pin_memory() for _ in range(slots)]
+        self.staging = [torch.empty((1 << 16, 8), dtype=torch.int32).pin_memory() for _ in range(slots)]
         self.free_slots = list(range(slots))
         self.batches = 0
         self.t0 = time.perf_counter()
@@ -180,7 +183,7 @@ class Server:
         stream = self.streams[slot]
         tp = [time.perf_counter()]
         with torch.cuda.stream(stream):
-            self._prepare(batch, scenes, dev)
+            self._prepare(batch, scenes, dev, slot)
             tp.append(time.perf_counter())
             offs = np.zeros(len(batch) + 1, dtype=np.uint64)
             for i, sc in enumerate(scenes):
@@ -197,7 +200,9 @@ class Server:
                 buf = self.pinned[slot][:total]
                 eng.pairs_into(buf, stream=stream)
                 eng.sync(stream)
-                allp = buf.numpy().view(np.uint32).copy()
+                allp = buf.numpy().view(np.uint32)
+                if self.copy_pairs:  # the pinned buffer is reused by the slot's next batch
+                    allp = allp.copy()
         tp.append(time.perf_counter())
         t_done = self.now()
         for i, r in enumerate(batch):
@@ -220,10 +225,13 @@ class Server:
             self.free_slots.append(slot)
             self.lock.notify_all()
 
-    def _prepare(self, batch, scenes, dev) -> None:
+    def _prepare(self, batch, scenes, dev, slot) -> None:
         """Apply updates and make the batch's scenes device-resident (on the
-        current stream)."""
+        current stream). The moved rows of every update in the batch go up
+        in one copy through the slot's page-locked staging buffer (free
+        again: the slot's previous batch ended with a stream synchronize)."""
         torch = self.torch
+        moved = []  # (scene, indices) of updates whose scene stays resident
         for r, sc in zip(batch, scenes):
             r.nboxes = sc.host.shape[0]
             if sc.shift < 0:  # first query of the scene: tune its cell size once
@@ -231,14 +239,29 @@ class Server:
             if r.kind == "update":  # move a fraction of the boxes (host master copy)
                 idx = move_indices(sc.host.shape[0], r.move_frac, r.move_seed)
                 gen.move3d(sc.host, idx, r.move_seed, r.move_sigma)
+                if sc.dev is not None:
+                    moved.append((sc, idx))
             if sc.dev is None:  # not on the device (new or dropped): upload it whole
                 sc.dev = torch.from_numpy(sc.host.view(np.int32)).to(dev, non_blocking=True)
-            elif r.kind == "update":  # upload the moved rows only
-                ti = torch.from_numpy(idx.astype(np.int64)).to(dev, non_blocking=True)
-                rows = torch.from_numpy(sc.host[idx].view(np.int32)).pin_memory()
-                sc.dev[ti] = rows.to(dev, non_blocking=True)
             if self.keep_snapshots:
                 r.snapshot = sc.host.copy()
+        if moved:
+            k = sum(idx.shape[0] for _, idx in moved)
+            if self.staging[slot].shape[0] < k:
+                self.staging[slot] = torch.empty((int(k * 1.25) + 1024, 8), dtype=torch.int32).pin_memory()
+            st = self.staging[slot][:k].numpy()
+            a = 0
+            for sc, idx in moved:  # row = [7 coordinate/rid words, box index]
+                b = a + idx.shape[0]
+                np.take(sc.host.view(np.int32), idx, axis=0, out=st[a:b, :7])
+                st[a:b, 7] = idx.view(np.int32)
+                a = b
+            up = self.staging[slot][:k].to(dev, non_blocking=True)
+            a = 0
+            for sc, idx in moved:
+                b = a + idx.shape[0]
+                sc.dev.index_copy_(0, up[a:b, 7].long(), up[a:b, :7])
+                a = b
 
     # ---- dispatcher ----------------------------------------------------------
     def serve(self, n_expected: int, timeout: float = 600.0) -> None:
@@ -272,11 +295,7 @@ class Server:
 def move_indices(n: int, frac: float, seed: int) -> np.ndarray:
     """round(frac * n) (at least 1) distinct box indices, seeded, sorted."""
     k = min(n, max(1, int(round(frac * n))))
-    rng = np.random.default_rng(seed)
-    idx = np.unique(rng.integers(0, n, size=k + k // 4 + 8))
-    while idx.shape[0] < k:
-        idx = np.unique(np.concatenate([idx, rng.integers(0, n, size=k)]))
-    return np.sort(rng.permutation(idx)[:k]).astype(np.uint32)
+    return gen.pick(n, k, seed)
 
 
 def pinned_boxes(n: int) -> np.ndarray:

@@ -34,6 +34,24 @@ def test_own_math_accuracy():
         assert abs(L.pbig_gen_exp(x) - math.exp(x)) <= 1e-14 * math.exp(x)
     for u in np.linspace(0, 1, 1001, endpoint=False):
         assert abs(L.pbig_gen_cos2pi(u) - math.cos(2 * math.pi * u)) <= 1e-14
+        assert abs(L.pbig_gen_cos2pi_nodiv(u) - math.cos(2 * math.pi * u)) <= 1e-14
+    for x in [1e-300, 1e-10, 0.1, 0.5, 0.75, 0.999999, 1.0]:
+        assert abs(L.pbig_gen_log_nodiv(x) - math.log(x)) <= 1e-15 * max(1.0, abs(math.log(x)))
+
+
+def test_update_moves():
+    from pbig_gb300 import serve
+    idx = serve.move_indices(150000, 0.01, 3)
+    assert len(idx) == 1500 and len(np.unique(idx)) == 1500 and np.all(np.diff(idx.astype(np.int64)) > 0)
+    assert idx.max() < 150000
+    assert len(serve.move_indices(7, 1.0, 1)) == 7 and len(serve.move_indices(256, 0.01, 1)) == 3
+    b0 = gen.scene3d(150000, 3)
+    b = b0.copy()
+    gen.move3d(b, idx, 5)
+    untouched = np.setdiff1d(np.arange(150000), idx)
+    assert np.array_equal(b[untouched], b0[untouched]) and np.array_equal(b[:, 6], b0[:, 6])
+    d = (b[idx, 0].astype(np.int64) - b0[idx, 0]) / gen.RANGE
+    assert abs(np.median(np.abs(d)) / 0.6745 - 0.001) < 1e-4  # N(0, 0.001) displacement
 
 
 def test_workload_shapes():
