@@ -242,7 +242,6 @@ static int ensure_query_buffers(pbig2_ctx* c, Params& p, uint64_t entry_cap, uin
         CK(c->d_scene_cursor.ensure((nsc + 1) * 8, false, st));
     }
     p.counts = c->d_counts.as<uint32_t>();
-    p.starts = c->d_starts.as<uint32_t>();
     p.entries = c->d_entries.as<uint32_t>();
     p.entry_cap = ecap;
     p.lists = c->d_lists.as<uint2>();
@@ -273,7 +272,6 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
     }
     if (full) {
         R(cudaMemsetAsync(p.ctr, 0, sizeof(Ctr), st));
-        R(cudaMemsetAsync(p.tile_state, 0, scan_tiles(p.ncells) * 8, st));
         R(cudaEventRecordWithFlags(c->evp[0], st, evf));
         R(launch_count(p, dims, st));
         R(cudaEventRecordWithFlags(c->evp[1], st, evf));
@@ -389,7 +387,7 @@ static int capture_graph(pbig2_ctx* c, const Params& p0, const uint32_t* d_boxes
     G.nscenes_cap = nsc;
     G.entry_cap = p.entry_cap;
     G.out_cap = p.out_cap;
-    G.launches = 10;
+    G.launches = 12;  // count, scan (3), expand, scatter, pairs (3), scene grouping (3)
     G.buffers = c->buffers_sig();
     return PBIG2_OK;
 }
@@ -463,7 +461,6 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         CK(cudaGraphLaunch(G.exec, st));
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
-            c->counts_dirty = true;
             return fail(PBIG2_ECUDA, "pipeline failed: %s", cudaGetErrorString(e));
         }
         memcpy(&h, c->h_ctr.p, sizeof(Ctr));
@@ -471,11 +468,10 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         const bool over = (h.err & (kErrEntryOvf | kErrTaskOvf | kErrOutOvf)) || h.entries > G.entry_cap ||
                           h.pairs > G.out_cap;
         if (h.err & kErrWait) {
-            c->counts_dirty = true;
-            return fail(PBIG2_ETIMEOUT, "scan look-back wait gave up");
+            return fail(PBIG2_ETIMEOUT, "a bounded device wait gave up (scan bulk copy)");
         }
         if (over) {
-            // the counts went back to zero; redo eagerly with larger buffers
+            // redo eagerly with larger buffers
             // and capture again next time
             c->drop_graph();
             c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
@@ -486,11 +482,8 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     }
 
     // ---- eager run (retries on capacity) ----
-    const bool counts_new = c->d_counts.bytes < ncells * 4;
-    CK(c->d_counts.ensure(ncells * 4, true, st));
-    if (c->counts_dirty && !counts_new) CK(cudaMemsetAsync(c->d_counts.p, 0, c->d_counts.bytes, st));
-    CK(c->d_starts.ensure((ncells + 1) * 4 + 16, false, st));
-    CK(c->d_state.ensure(scan_tiles(ncells) * 8, false, st));
+    CK(c->d_counts.ensure(ncells * 4 + 16, false, st));  // zeroed by every pass
+    CK(c->d_state.ensure(scan_state_bytes(ncells), false, st));
     CK(c->d_ctr.ensure(sizeof(Ctr), false, st));
     CK(c->h_ctr.ensure(sizeof(Ctr)));
 
@@ -512,7 +505,6 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     p.tile_state = c->d_state.as<unsigned long long>();
     p.ctr = c->d_ctr.as<Ctr>();
     p.dyn = nullptr;
-    c->counts_dirty = true;  // until a pass completes, counts may be non-zero
     bool need_full = true;
     for (int attempt = 0; attempt < 6; attempt++) {
         int rc = ensure_query_buffers(c, p, entry_cap, out_cap, task_cap, nsc, grouped, st);
@@ -523,22 +515,18 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
             if (re != cudaSuccess)
                 return fail(PBIG2_ECUDA, "pipeline launch (engine.cu:%d): %s", g_record_line, cudaGetErrorString(re));
         }
-        launches += need_full ? 4 : 0;
+        launches += need_full ? 6 : 0;  // count, scan (3), expand, scatter
         launches += 3 + (grouped ? 3 : 0);
         CK(cudaMemcpyAsync(c->h_ctr.p, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, st));
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
-            c->counts_dirty = true;
             return fail(PBIG2_ECUDA, "pipeline failed: %s", cudaGetErrorString(e));
         }
         memcpy(&h, c->h_ctr.p, sizeof(Ctr));
-        c->counts_dirty = false;  // the scatter returned every count to zero
         if (h.err & kErrWait) {
-            c->counts_dirty = true;
-            return fail(PBIG2_ETIMEOUT, "scan look-back wait gave up");
+            return fail(PBIG2_ETIMEOUT, "a bounded device wait gave up (scan bulk copy)");
         }
         if (h.err & kErrIndex) {
-            c->counts_dirty = true;
             return fail(PBIG2_ECUDA, "inconsistent cell lists (error bits 0x%x)", h.err);
         }
         if ((h.err & kErrEntryOvf) || h.entries > p.entry_cap) {
@@ -643,7 +631,7 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     cudaSetDevice(c->device);
     if (c->own_stream) cudaStreamSynchronize(c->own_stream);
     c->drop_graph();
-    for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_starts, &c->d_entries,
+    for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_entries,
                       &c->d_lists, &c->d_tasks, &c->d_state,
                       &c->d_out, &c->d_out2, &c->d_ctr, &c->d_scenes, &c->d_scene_off, &c->d_scene_pair,
                       &c->d_scene_cursor, &c->d_dims})

@@ -51,10 +51,9 @@ struct pbig2_ctx {
     cudaStream_t own_stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evp[9] = {};
-    pbig::DevBuf d_boxes, d_counts, d_starts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
+    pbig::DevBuf d_boxes, d_counts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
         d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims;
     pbig::HostPinned h_ctr, h_stage;
-    bool counts_dirty = false;
     // last result
     const uint2* result = nullptr;
     uint64_t npairs = 0;
@@ -75,7 +74,7 @@ struct pbig2_ctx {
     } graph;
     uintptr_t buffers_sig() const {
         uintptr_t h = 0;
-        for (const pbig::DevBuf* b : {&d_counts, &d_starts, &d_entries, &d_lists, &d_tasks, &d_state, &d_out, &d_out2,
+        for (const pbig::DevBuf* b : {&d_counts, &d_entries, &d_lists, &d_tasks, &d_state, &d_out, &d_out2,
                                       &d_ctr, &d_scenes, &d_scene_off, &d_scene_pair, &d_scene_cursor, &d_dims})
             h = h * 1000003u + (uintptr_t)b->p;
         return h * 1000003u + (uintptr_t)h_ctr.p;

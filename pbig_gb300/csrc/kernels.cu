@@ -152,8 +152,9 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
             const uint64_t gid = o_base + ((uint64_t)k * o_nrc + j) * o_nrc + i;
             if (SCATTER) {
                 const uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
-                const uint32_t slot = atomicSub(&p.counts[gid], 1u) - 1u;
-                const uint64_t pos = (uint64_t)p.starts[gid] + slot;
+                // after the scan a cell's counter holds its end: counting it
+                // down hands out the cell's slots (and leaves its start)
+                const uint64_t pos = (uint64_t)(atomicSub(&p.counts[gid], 1u) - 1u);
                 if (pos < p.entry_cap) p.entries[pos] = (f << kIdBits) | (uint32_t)(wbox0 + o);
                 else atomicOr(&p.ctr->err, kErrEntryOvf);
             } else {
@@ -161,6 +162,16 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
             }
         }
     }
+}
+
+// counts = 0 before a pass (the scatter leaves every cell's start there)
+__global__ void k_zero_counts(Params pin) {
+    const Params p = resolve(pin);
+    const uint64_t n4 = p.ncells / 4;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint4* c4 = reinterpret_cast<uint4*>(p.counts);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) c4[i] = make_uint4(0, 0, 0, 0);
+    for (uint64_t i = 4 * n4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.ncells; i += stride) p.counts[i] = 0;
 }
 
 template <int D>
@@ -190,185 +201,337 @@ __global__ void __launch_bounds__(kBoxThreads) k_scatter(Params pin) {
 }
 
 // ---------------------------------------------------------------------------
-// scan: single-pass exclusive scan with decoupled look-back. A tile is 4096
-// cells: each warp owns 512 consecutive cells as 4 rows of 128, a lane 4
-// consecutive cells per row (one 16-byte load). Tile order is taken from an
-// atomic ticket so every tile only waits on tiles already running. The same
-// pass classifies cells into the work lists of the pair kernel.
+// scan: counts -> cell starts and the work lists of the pair kernels, in
+// three launches without inter-block waits.
+//
+// A tile is 4096 cells, a chunk 512 of them; every warp works on whole
+// chunks with no block barrier, so the loads of all resident warps are in
+// flight together. Tile records (64 bytes, zeroed before the scan) collect
+// per-chunk entry sums and per-tile totals.
+//
+//   k_scan_reduce  chunk entry total (stored per chunk, added to the tile)
+//                  and the pair tests of its cells (added to the tile);
+//                  two chunks per warp iteration, so eight 16-byte loads
+//                  per lane are in flight together.
+//   k_scan_prefix  one block: tile entry totals -> exclusive prefixes; the
+//                  entry and pair-test totals go to the counters.
+//   k_scan_cells   the same chunks again: starts from the tile prefix, the
+//                  tile's earlier chunks and a warp scan; every cell of two
+//                  or more boxes goes to its work list, a chunk reserving
+//                  its places with one atomic per list (list order is free).
+//
+// Lane l of a warp owns the 4 cells at 4l of each of the chunk's 4 rows of
+// 128 cells, so each 16-byte load or store of a warp covers 512 contiguous
+// bytes. The work list of a cell of n >= 2 boxes is 2..4, 5..8, 9..16,
+// 17..32, 33..128, 129..512 or more boxes; per-lane list counts travel
+// packed in 10-bit fields (a chunk has at most 512 cells per list).
 // ---------------------------------------------------------------------------
 constexpr int kScanThreads = 256;
-constexpr int kScanTile = 4096;
-constexpr unsigned long long kFlagAgg = 1ull << 62, kFlagPre = 2ull << 62;
-constexpr unsigned long long kValMask = (1ull << 62) - 1;
-constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr int kScanPerThread = 16;
+constexpr int kScanChunk = 32 * kScanPerThread;              // cells per warp item
+constexpr int kScanChunks = 8;                               // chunks per tile
+constexpr int kScanTile = kScanChunk * kScanChunks;
 
-__device__ __forceinline__ int list_of(uint32_t n) {
-    if (n < 2) return -1;
-    if (n <= 4) return 0;
-    if (n <= 8) return 1;
-    if (n <= 16) return 2;
-    if (n <= 32) return 3;
-    if (n <= kMedMax) return kListMed;
-    if (n <= kBigMax) return kListBig;
-    return kListHuge;
+struct TileRec {                         // 64 bytes per tile
+    unsigned long long sum;              // entries; exclusive prefix after k_scan_prefix
+    unsigned long long tests;            // pair tests of the tile's cells
+    uint32_t chunk[kScanChunks];         // entries per chunk
+    uint32_t pad[4];
+};
+static_assert(sizeof(TileRec) == 64, "tile record layout");
+
+static_assert(kMedMax == 128 && kBigMax == 512, "list bounds are powers of two");
+constexpr unsigned long long kClassByLog = 0x6666665544321000ull;  // nibble L: list of ceil(log2 n) = L
+__device__ __forceinline__ uint32_t class_of(uint32_t n) {
+    const uint32_t lg = 32u - __clz(n - 1u);  // ceil(log2 n) for n >= 2
+    return (uint32_t)(kClassByLog >> (4u * min(lg, 15u))) & 15u;
 }
 
-__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* a) {
-    return *reinterpret_cast<const volatile unsigned long long*>(a);
-}
-__device__ __forceinline__ void st_volatile(unsigned long long* a, unsigned long long v) {
-    *reinterpret_cast<volatile unsigned long long*>(a) = v;
-}
-
-__global__ void __launch_bounds__(kScanThreads, 5) k_scan(Params pin) {
-    __shared__ uint32_t s_tile;
-    __shared__ unsigned long long s_warp_tot[8];
-    __shared__ unsigned long long s_prefix;
-    __shared__ uint32_t s_cls[kNumLists], s_cls_base[kNumLists];
-    __shared__ unsigned long long s_tests;
-    const Params p = resolve(pin);
-    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
-    const uint64_t tiles = (p.ncells + kScanTile - 1) / kScanTile;
-    // persistent: each block takes tiles in ticket order until none is left
-    for (;;) {
-    if (t == 0) {
-        s_tile = atomicAdd(&p.ctr->ticket, 1u);
-        s_tests = 0;
+__device__ __forceinline__ unsigned long long warp_incl_scan64(unsigned long long v) {
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(FULL_MASK, v, o);
+        if (lane_id() >= o) v += t;
     }
-    if (t < kNumLists) s_cls[t] = 0;
-    __syncthreads();
-    const uint64_t tile = s_tile;
-    if (tile >= tiles) break;
-    const uint64_t c_warp = tile * kScanTile + (uint64_t)warp * 512;  // first cell of this warp
-    // load 4 rows x 4 cells per lane
-    uint32_t v[16];
-    const bool full = tile * kScanTile + kScanTile <= p.ncells;
+    return v;
+}
+
+__device__ __forceinline__ uint64_t chunk_cell(uint64_t chunk, int r) {
+    return chunk * kScanChunk + (uint64_t)r * 128 + lane_id() * 4;
+}
+
+// the 16 counts of this lane's cells of the chunk (zeros past the end)
+__device__ __forceinline__ void scan_load(const Params& p, uint64_t chunk, uint32_t v[kScanPerThread]) {
+    const bool full = chunk * kScanChunk + kScanChunk <= p.ncells;
 #pragma unroll
     for (int r = 0; r < 4; r++) {
-        const uint64_t c = c_warp + (uint64_t)r * 128 + lane * 4;
+        const uint64_t c = chunk_cell(chunk, r);
         if (full) {
-            const uint4 q = __ldcs(reinterpret_cast<const uint4*>(p.counts + c));
+            const uint4 q = *reinterpret_cast<const uint4*>(p.counts + c);
             v[4 * r] = q.x; v[4 * r + 1] = q.y; v[4 * r + 2] = q.z; v[4 * r + 3] = q.w;
         } else {
 #pragma unroll
-            for (int k = 0; k < 4; k++) v[4 * r + k] = (c + k < p.ncells) ? p.counts[c + k] : 0u;
+            for (int k = 0; k < 4; k++) v[4 * r + k] = c + k < p.ncells ? p.counts[c + k] : 0u;
         }
     }
-    // per-row lane sums and warp scans (64-bit running totals)
-    unsigned long long row_excl[4];
-    unsigned long long wtot = 0;
+}
+
+__device__ __forceinline__ void reduce_chunk(TileRec* rec, uint64_t ch, const uint32_t v[kScanPerThread]) {
+    const uint32_t lane = lane_id();
+    uint32_t lsum = 0, big = 0;  // < 2^32 while the entry total is
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const uint32_t s = v[4 * r] + v[4 * r + 1] + v[4 * r + 2] + v[4 * r + 3];
-        // lane sums fit 32 bits for < 2^30 boxes per cell
-        const uint32_t inc = warp_incl_scan(s);
-        row_excl[r] = wtot + (inc - s);
-        wtot += __shfl_sync(FULL_MASK, inc, 31);
+    for (int k = 0; k < kScanPerThread; k++) {
+        lsum += v[k];
+        big |= v[k] >> 1;
     }
-    if (lane == 0) s_warp_tot[warp] = wtot;
-    __syncthreads();
-    unsigned long long warp_excl = 0, agg = 0;
+    lsum = __reduce_add_sync(FULL_MASK, lsum);
+    TileRec& r = rec[ch / kScanChunks];
+    if (lane == 0) {
+        r.chunk[ch % kScanChunks] = lsum;
+        if (lsum) atomicAdd(&r.sum, (unsigned long long)lsum);
+    }
+    if (__any_sync(FULL_MASK, big != 0)) {
+        unsigned long long tests = 0;
 #pragma unroll
-    for (int w = 0; w < 8; w++) {
-        const unsigned long long x = s_warp_tot[w];
-        if (w < (int)warp) warp_excl += x;
-        agg += x;
+        for (int k = 0; k < kScanPerThread; k++)
+            if (v[k] >= 2u) tests += (unsigned long long)v[k] * (v[k] - 1u) / 2u;
+        tests = warp_sum_u64(tests);
+        if (lane == 0 && tests) atomicAdd(&r.tests, tests);
     }
-    // decoupled look-back (warp 0)
-    if (warp == 0) {
-        unsigned long long excl = 0;
-        if (tile == 0) {
-            if (lane == 0) st_volatile(&p.tile_state[0], kFlagPre | agg);
-        } else {
-            if (lane == 0) st_volatile(&p.tile_state[tile], kFlagAgg | agg);
-            long long look = (long long)tile - 1;
-            uint32_t spins = 0;
-            for (;;) {
-                const long long idx = look - (long long)lane;  // lane 0: nearest predecessor
-                const unsigned long long s = idx >= 0 ? ld_volatile(&p.tile_state[idx]) : kFlagPre;
-                const uint32_t notready = __ballot_sync(FULL_MASK, (s >> 62) == 0);
-                const uint32_t pm = __ballot_sync(FULL_MASK, (s >> 62) == 2);
-                // done at the nearest inclusive prefix once every nearer tile has
-                // published its aggregate; a window without one is summed whole
-                const uint32_t first = pm ? (uint32_t)(__ffs(pm) - 1) : 32u;
-                const uint32_t need = first == 32u ? 0xffffffffu : ((1u << first) - 1u);
-                if ((notready & need) == 0) {
-                    excl += warp_sum_u64(lane <= first ? (s & kValMask) : 0ull);
-                    if (pm) break;
-                    look -= 32;
-                    continue;
-                }
-                if (++spins > kSpinLimit) {
-                    if (lane == 0) atomicOr(&p.ctr->err, kErrWait);
-                    break;
-                }
-                __nanosleep(64);
-            }
-            if (lane == 0) st_volatile(&p.tile_state[tile], kFlagPre | (excl + agg));
-        }
-        if (lane == 0) s_prefix = excl;
+}
+
+__global__ void __launch_bounds__(kScanThreads, 4) k_scan_reduce(Params pin) {
+    const Params p = resolve(pin);
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint64_t chunks = (p.ncells + kScanChunk - 1) / kScanChunk;
+    TileRec* rec = reinterpret_cast<TileRec*>(p.tile_state);
+    const uint64_t nw = (uint64_t)gridDim.x * (kScanThreads / 32);
+    for (uint64_t ch = 2 * ((uint64_t)blockIdx.x * (kScanThreads / 32) + warp); ch < chunks; ch += 2 * nw) {
+        uint32_t v[kScanPerThread], w[kScanPerThread];
+        scan_load(p, ch, v);
+        const bool two = ch + 1 < chunks;
+        if (two) scan_load(p, ch + 1, w);
+        reduce_chunk(rec, ch, v);
+        if (two) reduce_chunk(rec, ch + 1, w);
     }
-    __syncthreads();
-    const unsigned long long base = s_prefix + warp_excl;
-    // write starts and classify cells
-    uint32_t my_cls[kNumLists] = {0, 0, 0, 0, 0, 0, 0};
-    unsigned long long tests = 0;
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const uint64_t c = c_warp + (uint64_t)r * 128 + lane * 4;
-        unsigned long long run = base + row_excl[r];
-        uint32_t st[4];
+}
+
+constexpr int kPrefixThreads = 1024;
+__global__ void __launch_bounds__(kPrefixThreads) k_scan_prefix(Params pin) {
+    __shared__ unsigned long long s_part[kPrefixThreads / 32][2];
+    __shared__ unsigned long long s_carry[2];
+    const Params p = resolve(pin);
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    const uint64_t tiles = (p.ncells + kScanTile - 1) / kScanTile;
+    TileRec* rec = reinterpret_cast<TileRec*>(p.tile_state);
+    if (t == 0) s_carry[0] = s_carry[1] = 0;
+    // rounds of 4 tiles per thread: all loads of a round in flight together
+    for (uint64_t r0 = 0; r0 < tiles; r0 += 4 * kPrefixThreads) {
+        unsigned long long x[4], y[4], sx = 0, sy = 0;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            st[k] = (uint32_t)run;
-            run += v[4 * r + k];
-            const int cl = list_of(v[4 * r + k]);
-            if (cl >= 0) my_cls[cl]++;
-            tests += (unsigned long long)v[4 * r + k] * (v[4 * r + k] - (v[4 * r + k] ? 1u : 0u)) / 2;
+            const uint64_t i = r0 + 4 * (uint64_t)t + k;
+            x[k] = i < tiles ? rec[i].sum : 0ull;
+            y[k] = i < tiles ? rec[i].tests : 0ull;
+            sx += x[k];
+            sy += y[k];
         }
-        if (full) {
-            *reinterpret_cast<uint4*>(p.starts + c) = make_uint4(st[0], st[1], st[2], st[3]);
-        } else {
+        const unsigned long long ix = warp_incl_scan64(sx);
+        const unsigned long long iy = warp_sum_u64(sy);
+        if (lane == 31) s_part[warp][0] = ix;
+        if (lane == 0) s_part[warp][1] = iy;
+        __syncthreads();
+        unsigned long long wo = s_carry[0], tot = 0, tt = 0;
+        for (int w = 0; w < kPrefixThreads / 32; w++) {
+            const unsigned long long a = s_part[w][0];
+            if (w < (int)warp) wo += a;
+            tot += a;
+            tt += s_part[w][1];
+        }
+        unsigned long long run = wo + (ix - sx);
 #pragma unroll
-            for (int k = 0; k < 4; k++)
-                if (c + k < p.ncells) p.starts[c + k] = st[k];
+        for (int k = 0; k < 4; k++) {
+            const uint64_t i = r0 + 4 * (uint64_t)t + k;
+            if (i < tiles) rec[i].sum = run;
+            run += x[k];
         }
+        __syncthreads();
+        if (t == 0) {
+            s_carry[0] += tot;
+            s_carry[1] += tt;
+        }
+        __syncthreads();
     }
-    // tile end: the last tile writes starts[ncells] and the entry total
-    if (t == 0 && (tile + 1) * kScanTile >= p.ncells) {
-        const unsigned long long total = s_prefix + agg;
-        p.starts[p.ncells] = (uint32_t)total;
+    if (t == 0) {
+        const unsigned long long total = s_carry[0];
         p.ctr->entries = total;
+        p.ctr->tests = s_carry[1];
         if (total >= (1ull << 32)) atomicOr(&p.ctr->err, kErrEntryOvf);
     }
-    tests = warp_sum_u64(tests);
-    if (lane == 0 && tests) atomicAdd(&s_tests, tests);
-#pragma unroll
-    for (int c = 0; c < kNumLists; c++)
-        if (my_cls[c]) atomicAdd(&s_cls[c], my_cls[c]);
-    __syncthreads();
-    if (t < kNumLists) {
-        s_cls_base[t] = s_cls[t] ? atomicAdd(&p.ctr->n_list[t], s_cls[t]) : 0u;
-        s_cls[t] = 0;
+}
+
+// ---- bulk asynchronous copies (global -> shared) completing on an mbarrier
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// arm the barrier for `bytes` and copy them (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait for the phase of parity `parity`; false when it gave up
+constexpr uint32_t kBulkWaitLimit = 1u << 20;
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kBulkWaitLimit; i++)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+
+// k_scan_cells: each warp keeps its next chunk's counts in flight as a bulk
+// copy into one of two shared-memory buffers while it works on the current
+// one. A partial chunk (only the grid's last) is read with plain loads.
+__global__ void __launch_bounds__(kScanThreads, 4) k_scan_cells(Params pin) {
+    __shared__ __align__(128) uint32_t s_buf[kScanThreads / 32][2][kScanChunk];
+    __shared__ __align__(8) unsigned long long s_bar[kScanThreads / 32][2];
+    const Params p = resolve(pin);
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    const uint64_t chunks = (p.ncells + kScanChunk - 1) / kScanChunk;
+    const uint64_t full_chunks = p.ncells / kScanChunk;
+    const TileRec* rec = reinterpret_cast<const TileRec*>(p.tile_state);
+    const uint64_t nw = (uint64_t)gridDim.x * (kScanThreads / 32);
+    const uint64_t first = (uint64_t)blockIdx.x * (kScanThreads / 32) + warp;
+    if (lane == 0) {
+        mbar_init(&s_bar[warp][0], 1);
+        mbar_init(&s_bar[warp][1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (t == 0 && s_tests) atomicAdd(&p.ctr->tests, s_tests);
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const uint64_t c = c_warp + (uint64_t)r * 128 + lane * 4;
-        uint32_t run = (uint32_t)(base + row_excl[r]);
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int cl = list_of(v[4 * r + k]);
-            if (cl >= 0) {
-                const uint64_t idx = (uint64_t)s_cls_base[cl] + atomicAdd(&s_cls[cl], 1u);
-                if (idx < p.list_cap[cl]) p.lists[p.list_off[cl] + idx] = make_uint2(run, v[4 * r + k]);
+    __syncwarp();
+    auto issue = [&](uint64_t i) {  // chunk i of this warp into buffer i & 1
+        const uint64_t ch = first + i * nw;
+        if (lane == 0 && ch < full_chunks)
+            bulk_load(s_buf[warp][i & 1], p.counts + ch * kScanChunk, kScanChunk * 4, &s_bar[warp][i & 1]);
+    };
+    issue(0);
+    issue(1);
+    for (uint64_t i = 0;; i++) {
+        const uint64_t ch = first + i * nw;
+        if (ch >= chunks) break;
+        uint32_t v[kScanPerThread];
+        if (ch < full_chunks) {
+            if (!mbar_wait(&s_bar[warp][i & 1], (uint32_t)(i >> 1) & 1u)) {
+                // give up: report, wait (bounded) for the copy still in flight, stop
+                if (lane == 0) atomicOr(&p.ctr->err, kErrWait);
+                mbar_wait(&s_bar[warp][i & 1], (uint32_t)(i >> 1) & 1u);
+                if (first + (i + 1) * nw < full_chunks)
+                    mbar_wait(&s_bar[warp][(i + 1) & 1], (uint32_t)((i + 1) >> 1) & 1u);
+                return;
             }
-            run += v[4 * r + k];
+            const uint32_t* b = s_buf[warp][i & 1];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint4 x = *reinterpret_cast<const uint4*>(b + q * 128 + lane * 4);
+                v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
+            }
+            __syncwarp();
+            // the buffer's reads are done: it can take the chunk after next
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(i + 2);
+        } else {
+            scan_load(p, ch, v);
         }
-        (void)c;
-    }
-    __syncthreads();  // shared state is reused by the next tile
+        const TileRec& r = rec[ch / kScanChunks];
+        const uint32_t ci = (uint32_t)(ch % kScanChunks);
+        // entries before this chunk: tile prefix + the tile's earlier chunks
+        unsigned long long base = lane == 0 ? r.sum : 0ull;
+        if (lane > 0 && lane <= ci) base = r.chunk[lane - 1];
+        base = warp_sum_u64(base);
+        uint32_t big = 0;
+#pragma unroll
+        for (int k = 0; k < kScanPerThread; k++) big |= v[k] >> 1;
+        // row scans: the cells of row q before this lane's, and rows < q whole
+        uint32_t st[kScanPerThread];
+        const bool full = ch < full_chunks;
+        unsigned long long wtot = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t rs = v[4 * q] + v[4 * q + 1] + v[4 * q + 2] + v[4 * q + 3];
+            const uint32_t inc = warp_incl_scan(rs);  // < 2^32 while the entry total is
+            unsigned long long run = base + wtot + (inc - rs);
+            wtot += __shfl_sync(FULL_MASK, inc, 31);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                st[4 * q + k] = (uint32_t)run;
+                run += v[4 * q + k];
+            }
+            // the cell's counter becomes its end (start + count), in place
+            const uint64_t c = chunk_cell(ch, q);
+            if (full) {
+                *reinterpret_cast<uint4*>(p.counts + c) = make_uint4(
+                    st[4 * q] + v[4 * q], st[4 * q + 1] + v[4 * q + 1], st[4 * q + 2] + v[4 * q + 2], st[4 * q + 3] + v[4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (c + k < p.ncells) p.counts[c + k] = st[4 * q + k] + v[4 * q + k];
+            }
+        }
+        if (__any_sync(FULL_MASK, big != 0)) {
+            // per-lane list counts: lists 0..5 in 10-bit fields of pk, list 6 in pk6
+            unsigned long long pk = 0;
+            uint32_t pk6 = 0;
+#pragma unroll
+            for (int k = 0; k < kScanPerThread; k++) {
+                if (v[k] >= 2u) {
+                    const uint32_t c = class_of(v[k]);
+                    if (c < 6u) pk += 1ull << (10u * c);
+                    else pk6 += 1u;
+                }
+            }
+            const unsigned long long pinc = warp_incl_scan64(pk);
+            const uint32_t p6inc = warp_incl_scan(pk6);
+            unsigned long long pk_excl = pinc - pk;
+            uint32_t pk6_excl = p6inc - pk6;
+            // lane c < 7: this chunk's first place in list c
+            const unsigned long long ptot = __shfl_sync(FULL_MASK, pinc, 31);
+            const uint32_t p6tot = __shfl_sync(FULL_MASK, p6inc, 31);
+            uint32_t lbase = 0;
+            if (lane < kNumLists) {
+                const uint32_t x = lane < 6u ? (uint32_t)(ptot >> (10u * lane)) & 1023u : p6tot;
+                if (x) lbase = atomicAdd(&p.ctr->n_list[lane], x);
+            }
+#pragma unroll
+            for (int k = 0; k < kScanPerThread; k++) {
+                const uint32_t c = v[k] >= 2u ? class_of(v[k]) : 0u;
+                const uint32_t b = __shfl_sync(FULL_MASK, lbase, c);
+                if (v[k] >= 2u) {
+                    uint32_t rk;
+                    if (c < 6u) {
+                        rk = (uint32_t)(pk_excl >> (10u * c)) & 1023u;
+                        pk_excl += 1ull << (10u * c);
+                    } else {
+                        rk = pk6_excl++;
+                    }
+                    const uint64_t idx = (uint64_t)b + rk;
+                    if (idx < pin.list_cap[c]) p.lists[pin.list_off[c] + idx] = make_uint2(st[k], v[k]);
+                }
+            }
+        }
     }
 }
 
@@ -1101,6 +1264,7 @@ static unsigned box_grid(uint64_t nboxes) {
 }
 
 cudaError_t launch_count(const Params& p, int dims, cudaStream_t st) {
+    k_zero_counts<<<(unsigned)((g_sm_count > 0 ? g_sm_count : 152) * 4), 512, 0, st>>>(p);
     const unsigned g = box_grid(p.nboxes);
     if (g == 0) return cudaSuccess;
     if (dims == 2) k_count<2><<<g, kBoxThreads, 0, st>>>(p);
@@ -1117,11 +1281,20 @@ cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st) {
 }
 
 cudaError_t launch_scan(const Params& p, cudaStream_t st) {
-    const uint64_t tiles = scan_tiles(p.ncells);
-    const uint64_t cap = (uint64_t)(g_sm_count > 0 ? g_sm_count : 152) * 5;
-    k_scan<<<(unsigned)(tiles < cap ? (tiles ? tiles : 1) : cap), kScanThreads, 0, st>>>(p);
+    const uint64_t chunks = (p.ncells + kScanChunk - 1) / kScanChunk;
+    const uint64_t blocks = (chunks + kScanThreads / 32 - 1) / (kScanThreads / 32);
+    const uint64_t cap = (uint64_t)(g_sm_count > 0 ? g_sm_count : 152) * 4;  // resident: 4 blocks per SM
+    const unsigned g = (unsigned)(blocks < cap ? (blocks ? blocks : 1) : cap);
+    const unsigned g2 = (unsigned)((blocks + 1) / 2 < cap ? ((blocks + 1) / 2 ? (blocks + 1) / 2 : 1) : cap);
+    cudaError_t e = cudaMemsetAsync(p.tile_state, 0, scan_state_bytes(p.ncells), st);
+    if (e != cudaSuccess) return e;
+    k_scan_reduce<<<g2, kScanThreads, 0, st>>>(p);
+    k_scan_prefix<<<1, kPrefixThreads, 0, st>>>(p);
+    k_scan_cells<<<g, kScanThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
+
+size_t scan_state_bytes(uint64_t ncells) { return scan_tiles(ncells) * sizeof(TileRec); }
 
 cudaError_t launch_scene_offsets(const Params& p, const unsigned long long* hist, unsigned long long* off,
                                  uint32_t nscenes_cap, cudaStream_t st) {

@@ -73,8 +73,7 @@ struct Params {
     uint32_t nscenes;
     uint32_t split;               // bipartite: global index of the first blue box
     uint32_t max_range;           // largest scene range (selects the pair-test arithmetic)
-    uint32_t* counts;             // [ncells] (zero before count; zero after scatter)
-    uint32_t* starts;             // [ncells+1] exclusive scan of counts
+    uint32_t* counts;             // [ncells] per-cell counts; cell ends after the scan, starts after the scatter
     uint64_t ncells;
     uint32_t* entries;            // [entry_cap]: flags<<29 | global box index
     uint64_t entry_cap;
@@ -83,7 +82,7 @@ struct Params {
     uint64_t list_cap[kNumLists];
     uint4* tasks;                 // huge-cell tile tasks {start, n, r, x0}
     uint64_t task_cap;
-    unsigned long long* tile_state; // scan look-back state, one per tile
+    unsigned long long* tile_state; // scan tile records (128 bytes per 4096 cells)
     uint2* out;                   // pairs
     uint64_t out_cap;
     Ctr* ctr;
@@ -108,6 +107,7 @@ cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* sce
                                   unsigned long long* scene_cursor, uint2* dst, cudaStream_t st);
 cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st);
 uint64_t scan_tiles(uint64_t ncells);
+size_t scan_state_bytes(uint64_t ncells);  // scan tile records
 size_t pair_smem_bytes();
 cudaError_t kernels_init();
 

@@ -6,7 +6,7 @@
 // latency-critical loop that cannot afford cudaMalloc/cudaFree, which may
 // synchronize the whole device. For them this entry point runs the same
 // kernels as pbig2_self_intersect but keeps every intermediate buffer (cell
-// counts and starts, cell entries, work lists, tile tasks, scan state,
+// counts, cell entries, work lists, tile tasks, scan state,
 // counters) in one fixed scratch array that is part of the library image.
 // The caller passes device-resident boxes and a device output buffer; the
 // call allocates nothing.
@@ -133,10 +133,9 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
     Scene* scene = (Scene*)take(sizeof(Scene));
     uint32_t* scene_off = (uint32_t*)take(2 * sizeof(uint32_t));
     p.ctr = (Ctr*)take(sizeof(Ctr));
-    p.counts = (uint32_t*)take(ncells * 4);
-    p.starts = (uint32_t*)take((ncells + 1) * 4 + 16);
+    p.counts = (uint32_t*)take(ncells * 4 + 16);
     const uint64_t tiles = scan_tiles(ncells);
-    p.tile_state = (unsigned long long*)take(tiles * 8);
+    p.tile_state = (unsigned long long*)take(scan_state_bytes(ncells));
     p.entries = (uint32_t*)take(kNaMaxEntries * 4);
     p.entry_cap = kNaMaxEntries;
     const uint64_t lo[kNumLists] = {2, 5, 9, 17, 33, kMedMax + 1, kBigMax + 1};
@@ -174,8 +173,6 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
     e = cudaMemcpyAsync(scene, &sc, sizeof(Scene), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(scene_off, offs, sizeof offs, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p.ctr, 0, sizeof(Ctr), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(p.counts, 0, ncells * 4, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(p.tile_state, 0, tiles * 8, st);
     if (e == cudaSuccess) e = launch_count(p, (int)dims, st);
     if (e == cudaSuccess) e = launch_scan(p, st);
     if (e == cudaSuccess) e = launch_expand(p, st);
@@ -189,7 +186,7 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
     if (e != cudaSuccess) return na_fail(PBIG2_ECUDA, "pipeline", e);
     *npairs = h.pairs;
     if (h.err & (kErrEntryOvf | kErrTaskOvf)) return na_fail(PBIG2_ECAPACITY, "scene needs more cell entries than the scratch holds (limit 524288)");
-    if (h.err & kErrWait) return na_fail(PBIG2_ETIMEOUT, "scan look-back wait gave up");
+    if (h.err & kErrWait) return na_fail(PBIG2_ETIMEOUT, "a bounded device wait gave up (scan bulk copy)");
     if (h.err & kErrIndex) return na_fail(PBIG2_ECUDA, "inconsistent cell lists");
     if (h.pairs > pair_cap) return na_fail(PBIG2_ECAPACITY, "pair buffer too small; *npairs holds the pair count");
     if (h.bad) return na_fail(PBIG2_EINPUT, "some boxes violate the input contract and were skipped");
