@@ -109,13 +109,27 @@ PBIG2_API int pbig2_batch_intersect(pbig2_ctx* ctx, const uint32_t* boxes,
                                     uint32_t range, const uint32_t* cell_shifts, int boxes_loc,
                                     void* stream, uint64_t* npairs);
 
-/* Result of the last query: device pointer to npairs uint32 pairs
- * (a<b for self queries; (red,blue) for bipartite), valid until the next
- * query on the context. */
+/* Result of the last query: pointer to npairs uint32 pairs (a<b for self
+ * queries; (red,blue) for bipartite), valid until the next query on the
+ * context -- the context's device buffer, or the caller's buffer given to
+ * pbig2_set_pair_output when the pairs went there. */
 PBIG2_API int pbig2_result_pairs(pbig2_ctx* ctx, const uint32_t** dev_pairs, uint64_t* npairs);
 
+/* Direct pair output (no counterpart in the reference, whose decode() always
+ * copies batches out). Later self and bipartite queries on ctx store their
+ * pairs straight into dst, cap_pairs pairs of it: device memory, or
+ * page-locked host memory (pbig2_host_alloc) that the pair kernels write
+ * over the host link while they run, so no separate device-to-host copy is
+ * needed. A result of more than cap_pairs pairs is redone into the context's
+ * own device buffer (pbig2_result_pairs says where the pairs are; the copy
+ * functions work from either). dst = NULL restores the default. Batched
+ * queries always use the context's buffers. dst must stay valid while it is
+ * set. */
+PBIG2_API int pbig2_set_pair_output(pbig2_ctx* ctx, uint32_t* dst, uint64_t cap_pairs);
+
 /* Copy pairs [first, first+count) of the last result into dst (host or
- * device memory), in the result's order. */
+ * device memory), in the result's order; nothing to do when dst is where
+ * the result already is. */
 PBIG2_API int pbig2_copy_pairs(pbig2_ctx* ctx, uint32_t* dst, uint64_t first, uint64_t count,
                                int dst_loc, void* stream);
 

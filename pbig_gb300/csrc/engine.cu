@@ -307,7 +307,7 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
 static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t ncells, uint32_t nsc,
                         const std::vector<GridScene>& scenes, bool grouped, int launches, cudaStream_t st) {
     c->npairs = h.pairs;
-    c->result = grouped ? c->d_out2.as<uint2>() : c->d_out.as<uint2>();
+    c->result = grouped ? c->d_out2.as<uint2>() : c->result_ext ? c->ext_out : c->d_out.as<uint2>();
     if (grouped) {
         CK(c->h_stage.ensure((nsc + 1) * 8));
         CK(cudaMemcpyAsync(c->h_stage.p, c->d_scene_pair.p, (nsc + 1) * 8, cudaMemcpyDeviceToHost, st));
@@ -506,9 +506,17 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     p.ctr = c->d_ctr.as<Ctr>();
     p.dyn = nullptr;
     bool need_full = true;
+    // self/bipartite pairs go straight to the caller's buffer when one is set;
+    // a result that does not fit is redone into the context's buffer
+    bool use_ext = c->ext_out != nullptr && !grouped;
+    c->result_ext = false;
     for (int attempt = 0; attempt < 6; attempt++) {
-        int rc = ensure_query_buffers(c, p, entry_cap, out_cap, task_cap, nsc, grouped, st);
+        int rc = ensure_query_buffers(c, p, entry_cap, use_ext ? 1 : out_cap, task_cap, nsc, grouped, st);
         if (rc) return rc;
+        if (use_ext) {
+            p.out = c->ext_out;
+            p.out_cap = c->ext_cap;
+        }
         if (attempt == 0) CK(cudaEventRecord(c->ev0, st));
         {
             const cudaError_t re = record_pipeline(c, p, dims, grouped, nsc, need_full, st);
@@ -543,12 +551,14 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
             continue;
         }
         if ((h.err & kErrOutOvf) || h.pairs > p.out_cap) {
-            out_cap = h.pairs + h.pairs / 8 + 1024;
+            out_cap = std::max<uint64_t>(out_cap, h.pairs + h.pairs / 8 + 1024);
+            use_ext = false;
             need_full = false;
             continue;
         }
         break;
     }
+    c->result_ext = use_ext;
     if (h.err & (kErrEntryOvf | kErrTaskOvf | kErrOutOvf)) return fail(PBIG2_ENOMEM, "capacity retries exhausted");
     c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
     int rc = finish_query(c, h, nboxes, ncells, nsc, scenes, grouped, launches, st);
@@ -825,8 +835,9 @@ PBIG2_API int pbig2_copy_pairs(pbig2_ctx* c, uint32_t* dst, uint64_t first, uint
     if (count == 0) return PBIG2_OK;
     CK(cudaSetDevice(c->device));
     cudaStream_t st = pick_stream(c, stream);
-    const cudaMemcpyKind k = dst_loc == PBIG2_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    CK(cudaMemcpyAsync(dst, c->result + first, count * 8, k, st));
+    if ((const void*)dst == (const void*)(c->result + first)) return PBIG2_OK;  // already there
+    // the result is in device memory or in the caller's page-locked buffer
+    CK(cudaMemcpyAsync(dst, c->result + first, count * 8, cudaMemcpyDefault, st));
     if (dst_loc != PBIG2_DEVICE) CK(cudaStreamSynchronize(st));
     return PBIG2_OK;
 }
@@ -837,8 +848,29 @@ PBIG2_API int pbig2_copy_pairs_async(pbig2_ctx* c, uint32_t* dst, uint64_t first
     if (first > c->npairs || count > c->npairs - first) return fail(PBIG2_EINVAL, "range beyond the result");
     if (count == 0) return PBIG2_OK;
     CK(cudaSetDevice(c->device));
-    const cudaMemcpyKind k = dst_loc == PBIG2_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    CK(cudaMemcpyAsync(dst, c->result + first, count * 8, k, pick_stream(c, stream)));
+    (void)dst_loc;
+    if ((const void*)dst == (const void*)(c->result + first)) return PBIG2_OK;  // already there
+    CK(cudaMemcpyAsync(dst, c->result + first, count * 8, cudaMemcpyDefault, pick_stream(c, stream)));
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_set_pair_output(pbig2_ctx* c, uint32_t* dst, uint64_t cap_pairs) {
+    if (!c || (dst && cap_pairs == 0)) return fail(PBIG2_EINVAL, "bad arguments");
+    if (dst) {
+        // the pair kernels store into dst: it must be device memory or
+        // page-locked host memory mapped into the device's address space
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, dst) != cudaSuccess || a.type == cudaMemoryTypeUnregistered ||
+            a.devicePointer == nullptr) {
+            (void)cudaGetLastError();
+            return fail(PBIG2_EINVAL, "pair output must be device memory or page-locked (pbig2_host_alloc) host memory");
+        }
+        if (((uintptr_t)dst & 7u) != 0) return fail(PBIG2_EINVAL, "pair output must be 8-byte aligned");
+        c->ext_out = reinterpret_cast<uint2*>(a.devicePointer);
+    } else {
+        c->ext_out = nullptr;
+    }
+    c->ext_cap = dst ? cap_pairs : 0;
     return PBIG2_OK;
 }
 

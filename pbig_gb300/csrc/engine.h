@@ -54,6 +54,10 @@ struct pbig2_ctx {
     pbig::DevBuf d_boxes, d_counts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
         d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims;
     pbig::HostPinned h_ctr, h_stage;
+    // caller's pair buffer for self/bipartite queries (pbig2_set_pair_output)
+    uint2* ext_out = nullptr;
+    uint64_t ext_cap = 0;
+    bool result_ext = false;  // the last result went to ext_out
     // last result
     const uint2* result = nullptr;
     uint64_t npairs = 0;

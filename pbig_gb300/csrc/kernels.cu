@@ -581,7 +581,9 @@ __global__ void k_expand(Params p) {
 constexpr int kPairThreads = 256;
 constexpr int kPairWarps = kPairThreads / 32;
 constexpr uint32_t kMissShift = 29;
-constexpr uint32_t kWarpOut = 256;          // per-warp output buffer (pairs)
+constexpr uint32_t kWarpOut = 256;          // per-warp output buffer (pairs), small cells
+constexpr uint32_t kMedOut = 512;           // per-warp output buffer (pairs), medium cells: above the
+                                            // typical output of one emission step, so it rarely spills
 constexpr uint32_t kSmallSlots = 32;        // per-warp staging, small cells
 constexpr uint32_t kMedSlots = kMedMax;     // per-warp staging, medium cells
 constexpr uint32_t kBlockSlots = kBigMax;   // per-block staging, big cells
@@ -697,7 +699,8 @@ __device__ __forceinline__ uint32_t sweep_cols(const Slots& s, const Box& me, ui
 // ---- output: warp-private buffer ------------------------------------------
 struct WarpOut {
     uint2* buf;
-    uint32_t n;  // warp-uniform fill
+    uint32_t n;    // warp-uniform fill
+    uint32_t cap;  // buffer capacity (pairs)
 };
 
 __device__ __forceinline__ void wflush(const Params& p, WarpOut& o) {
@@ -729,9 +732,9 @@ __device__ __forceinline__ void wemit(const Params& p, WarpOut& o, uint32_t ma, 
     if (total == 0) return;
     bool direct = false;
     unsigned long long gbase = 0;
-    if (o.n + total > kWarpOut) {
+    if (o.n + total > o.cap) {
         wflush(p, o);
-        if (total > kWarpOut) {
+        if (total > o.cap) {
             direct = true;
             if (lane == 0) gbase = atomicAdd(&p.ctr->pairs, (unsigned long long)total);
             gbase = __shfl_sync(FULL_MASK, gbase, 0);
@@ -863,7 +866,7 @@ __global__ void __launch_bounds__(kPairThreads, 6) k_pairs_small(Params p) {
     __shared__ uint2 s_out[kPairWarps][kWarpOut];
     const uint32_t warp = threadIdx.x >> 5;
     const Slots s{s_a[warp], s_b[warp]};
-    WarpOut o{s_out[warp], 0};
+    WarpOut o{s_out[warp], 0, kWarpOut};
     const uint64_t gw = (uint64_t)blockIdx.x * kPairWarps + warp, nw = (uint64_t)gridDim.x * kPairWarps;
     // classes interleaved over the warps so every warp gets a similar mix
     small_items<D, 32, BIP, NARROW>(p, s, o, 3, gw, nw);
@@ -874,23 +877,124 @@ __global__ void __launch_bounds__(kPairThreads, 6) k_pairs_small(Params p) {
 }
 
 // ---- medium cells: one per warp item, staged whole ---------------------------
+// The reference-cell rule and the red/blue rule are applied per 32-column
+// tile with ballots (bit j: column j may pair with this lane's row box), so
+// the per-pair work is the overlap test alone: six differences whose OR has
+// bit 31 set iff some pair of intervals is disjoint, pushed into the hit
+// mask with one funnel shift (mask = mask << 1 | hit).
+
+// columns [c0, c0 + ncol) of the staged cell that row box `me` may pair with
+template <bool BIP>
+__device__ __forceinline__ uint32_t tile_allow(const Params& p, const Slots& s, uint32_t c0, uint32_t ncol,
+                                               const Box& me) {
+    const uint32_t lane = lane_id();
+    const bool v = lane < ncol;
+    const uint4 b = s.b[c0 + (v ? lane : 0u)];
+    const uint32_t f = v ? b.z >> kMissShift : 0u;
+    const uint32_t vm = __ballot_sync(FULL_MASK, v);
+    const uint32_t m0 = __ballot_sync(FULL_MASK, (f & 1u) != 0u);
+    const uint32_t m1 = __ballot_sync(FULL_MASK, (f & 2u) != 0u);
+    const uint32_t m2 = __ballot_sync(FULL_MASK, (f & 4u) != 0u);
+    const uint32_t fa = me.f >> kMissShift;
+    uint32_t allow = vm & ~(((fa & 1u) ? m0 : 0u) | ((fa & 2u) ? m1 : 0u) | ((fa & 4u) ? m2 : 0u));
+    if (BIP) {
+        const uint32_t red = __ballot_sync(FULL_MASK, v && b.w < p.split);
+        allow &= (me.id < p.split) ? ~red : red;
+    }
+    return allow;
+}
+
+// bit 31 set iff row box a and column box (ca, cz) are disjoint on some axis
+template <int D, bool NARROW>
+__device__ __forceinline__ uint32_t miss_word(const Box& a, const uint4& ca, const uint2& cz) {
+    if (NARROW) {
+        uint32_t t = (ca.y - a.x0) | (a.x1 - ca.x) | (ca.w - a.y0) | (a.y1 - ca.z);
+        if (D == 3) t |= (cz.y - a.z0) | (a.z1 - cz.x);
+        return t;
+    }
+    bool ok = (a.x0 <= ca.y) & (ca.x <= a.x1) & (a.y0 <= ca.w) & (ca.z <= a.y1);
+    if (D == 3) ok &= (a.z0 <= cz.y) & (cz.x <= a.z1);
+    return ok ? 0u : 0x80000000u;
+}
+
+__device__ __forceinline__ uint32_t push_hit(uint32_t mask, uint32_t miss) { return __funnelshift_l(~miss, mask, 1); }
+
+template <int D, bool NARROW>
+__device__ __forceinline__ uint32_t test_slot(const Slots& s, const Box& me, uint32_t mask, uint32_t i) {
+    const uint4 ca = s.a[i];
+    const uint2 cz = D == 3 ? *reinterpret_cast<const uint2*>(&s.b[i]) : make_uint2(0u, 0u);
+    return push_hit(mask, miss_word<D, NARROW>(me, ca, cz));
+}
+
+// row box against columns [c0, c0 + cnt), cnt a multiple of 8 up to 32;
+// bit cnt-1-j of the result: column j
+template <int D, bool NARROW>
+__device__ __forceinline__ uint32_t sweep_tile(const Slots& s, const Box& me, uint32_t c0, uint32_t cnt) {
+    uint32_t mask = 0;
+    if (cnt == 32) {
+#pragma unroll
+        for (uint32_t j = 0; j < 32; j++) mask = test_slot<D, NARROW>(s, me, mask, c0 + j);
+    } else {
+        for (uint32_t j0 = 0; j0 < cnt; j0 += 8) {
+#pragma unroll
+            for (uint32_t jj = 0; jj < 8; jj++) mask = test_slot<D, NARROW>(s, me, mask, c0 + j0 + jj);
+        }
+    }
+    return mask;
+}
+
+// circular half sweep of the m rows staged at [rb, rb + m): lane l < m tests
+// partners l+1 .. l+floor(m/2) (mod m), lanes past m/2 one fewer when m is
+// even (the BALANCE=1 sweep of d_matching, pbig.cu:804-825), so each
+// unordered pair is tested once; bit dmax-d of the result: partner l+d
+template <int D, bool NARROW>
+__device__ __forceinline__ uint32_t sweep_diag2(const Slots& s, const Box& me, uint32_t l, uint32_t rb, uint32_t m) {
+    uint32_t mask = 0;
+    if (m == 32) {
+#pragma unroll
+        for (uint32_t d = 1; d <= 16; d++) mask = test_slot<D, NARROW>(s, me, mask, rb + ((l + d) & 31u));
+    } else {
+        const uint32_t dmax = m >> 1;
+#pragma unroll 4
+        for (uint32_t d = 1; d <= dmax; d++) {
+            uint32_t pr = l + d;
+            if (pr >= m) pr -= m;
+            mask = test_slot<D, NARROW>(s, me, mask, rb + pr);
+        }
+    }
+    return mask;
+}
+
+// the allow mask of the diagonal tile in sweep_diag2's bit order, with the
+// half-sweep limit applied
+__device__ __forceinline__ uint32_t diag_allow(uint32_t allow, uint32_t lane, uint32_t m) {
+    if (lane >= m) return 0u;
+    const uint32_t dmax = m >> 1;
+    if (dmax == 0) return 0u;
+    uint32_t rot;  // bit d: partner (lane + d) mod m
+    if (m == 32) rot = __funnelshift_r(allow, allow, lane);
+    else rot = ((allow >> lane) | (allow << (m - lane))) & ((1u << m) - 1u);
+    uint32_t a = (__brev(rot) >> (31u - dmax)) & ((1u << dmax) - 1u);
+    if ((m & 1u) == 0u && lane >= dmax) a &= ~1u;  // even m: the opposite partner once
+    return a;
+}
+
 template <int D, bool BIP, bool NARROW>
 __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     uint4* base = reinterpret_cast<uint4*>(smem_raw);
     const Slots s{base + warp * 2 * kMedSlots, base + warp * 2 * kMedSlots + kMedSlots};
-    uint2* obuf = reinterpret_cast<uint2*>(base + kPairWarps * 2 * kMedSlots) + warp * kWarpOut;
-    WarpOut o{obuf, 0};
+    uint2* obuf = reinterpret_cast<uint2*>(base + kPairWarps * 2 * kMedSlots) + warp * kMedOut;
+    WarpOut o{obuf, 0, kMedOut};
     const uint64_t nl = mn64(p.ctr->n_list[kListMed], p.list_cap[kListMed]);
     const uint64_t nw = (uint64_t)gridDim.x * kPairWarps;
-    auto emit = [&](uint32_t ma, auto pa, uint32_t mb, auto pb, uint32_t myid) { wemit<BIP>(p, o, ma, pa, mb, pb, myid); };
     for (uint64_t item = (uint64_t)blockIdx.x * kPairWarps + warp; item < nl; item += nw) {
         const uint2 sn = p.lists[p.list_off[kListMed] + item];
         const uint32_t start = sn.x;
-        uint32_t n = sn.y;
+        const uint32_t n = sn.y;
         if (n > kMedMax || (uint64_t)start + n > p.entry_cap) continue;  // inconsistent grid: skip
-        const uint32_t n8 = (n + 7) & ~7u;
+        const uint32_t R = (n + 31) >> 5;
         // stage: all entry ids first, then all boxes (loads in flight together)
         uint32_t raw[kMedSlots / 32];
 #pragma unroll
@@ -901,11 +1005,41 @@ __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
 #pragma unroll
         for (uint32_t k = 0; k < kMedSlots / 32; k++) {
             const uint32_t e = lane + 32 * k;
-            if (e < n8) slot_put(s, e, e < n ? load_box<D, NARROW>(p, raw[k]) : dummy_box<NARROW>());
+            if (e < 32 * R) slot_put(s, e, e < n ? load_box<D, NARROW>(p, raw[k]) : dummy_box<NARROW>());
         }
         __syncwarp();
-        const uint32_t R = (n + 31) >> 5;
-        for (uint32_t r = 0; r < R; r++) row_unit<D, BIP, NARROW>(p, s, 0, n, r, emit);
+        for (uint32_t r = 0; r < R; r++) {
+            const uint32_t rows = min(32u, n - 32 * r), rb = 32 * r;
+            const Box me = slot_get(s, rb + lane);  // lanes >= rows hold a padding box, masked below
+            const uint32_t l = lane < rows ? lane : 0u;
+            const uint32_t dm = sweep_diag2<D, NARROW>(s, me, l, rb, rows) &
+                                diag_allow(tile_allow<BIP>(p, s, rb, rows, me), lane, rows);
+            const uint32_t dmax = rows >> 1;
+            auto pdiag = [&](uint32_t k) {
+                uint32_t pr = l + dmax - k;
+                if (pr >= rows) pr -= rows;
+                return slot_id(s, rb + pr);
+            };
+            uint32_t pend = dm;  // the diagonal's hits wait for the first column tile
+            bool have = true;
+            for (uint32_t x = r + 1; x < R; x++) {
+                const uint32_t c0 = 32 * x, ncol = min(32u, n - c0);
+                uint32_t allow = tile_allow<BIP>(p, s, c0, ncol, me);
+                if (lane >= rows) allow = 0u;
+                uint32_t mc = 0;
+                const uint32_t cnt = (ncol + 7) & ~7u;
+                if (__any_sync(FULL_MASK, allow != 0u))
+                    mc = sweep_tile<D, NARROW>(s, me, c0, cnt) & (__brev(allow) >> (32u - cnt));
+                auto pcol = [&](uint32_t k) { return slot_id(s, c0 + cnt - 1 - k); };
+                if (have) {
+                    wemit<BIP>(p, o, pend, pdiag, mc, pcol, me.id);
+                    have = false;
+                } else {
+                    wemit<BIP>(p, o, mc, pcol, 0u, pcol, me.id);
+                }
+            }
+            if (have) wemit<BIP>(p, o, pend, pdiag, 0u, pdiag, me.id);
+        }
         __syncwarp();
     }
     wflush(p, o);
@@ -1212,7 +1346,7 @@ __global__ void __launch_bounds__(1024) k_scene_offsets(Params pin, const unsign
 static int g_blocks_small = 1, g_blocks_med = 1, g_blocks_block = 1;
 static int g_sm_count = 0;
 
-static size_t med_smem() { return (size_t)kPairWarps * (2 * kMedSlots * sizeof(uint4) + kWarpOut * sizeof(uint2)); }
+static size_t med_smem() { return (size_t)kPairWarps * (2 * kMedSlots * sizeof(uint4) + kMedOut * sizeof(uint2)); }
 
 size_t pair_smem_bytes() { return sizeof(BlockSmem); }
 

@@ -3,10 +3,13 @@
 // Compiled together with the caller's report.h (it must be first on the
 // include path): pbig_check inlines report::operator() exactly as the
 // reference's decode() does (src/pbig/decode.cc:26-138, src/pbig/report.h:10),
-// so any report type a client defines keeps working. Pairs are streamed from
-// the device in chunks, the copy of chunk k+1 overlapping the callbacks of
-// chunk k (the reference's two-buffer match_phase pipeline,
-// src/pbig/pbig.cu:1694-1960, reduced to its output half).
+// so any report type a client defines keeps working. The pair kernels store
+// the pairs straight into a page-locked host buffer (pbig2_set_pair_output),
+// so the callbacks start as soon as the query returns; a result larger than
+// that buffer is streamed from the device in chunks instead, the copy of
+// chunk k+1 overlapping the callbacks of chunk k (the reference's two-buffer
+// match_phase pipeline, src/pbig/pbig.cu:1694-1960, reduced to its output
+// half), and the buffer grows for the next query.
 //
 // Errors follow the reference: CUDA failures print a message and exit(-1)
 // (src/pbig/log.h:4-12); boxes that break the input contract (coordinate >=
@@ -30,6 +33,8 @@ struct LegacyState {
     unsigned num = 0, range = 0;
     uint32_t shift = PBIG2_AUTO;
     uint32_t* chunk[2] = {nullptr, nullptr};
+    uint32_t* out = nullptr;  // direct pair output (page-locked)
+    uint64_t out_cap = 0;
     bool warned = false;
 };
 LegacyState g_state;
@@ -55,11 +60,27 @@ void pbig_finalize();
 
 void cuda_finalize() { pbig_finalize(); }
 
+static void set_out(uint64_t cap) {
+    if (g_state.out) {
+        pbig2_set_pair_output(g_state.ctx, nullptr, 0);
+        pbig2_host_free(g_state.out);
+        g_state.out = nullptr;
+        g_state.out_cap = 0;
+    }
+    if (pbig2_host_alloc(cap * 8, (void**)&g_state.out) != PBIG2_OK) die("pbig_init");
+    g_state.out_cap = cap;
+    if (pbig2_set_pair_output(g_state.ctx, g_state.out, cap) != PBIG2_OK) die("pbig_init");
+}
+
 void pbig_finalize() {
     for (auto& c : g_state.chunk) {
         if (c) pbig2_host_free(c);
         c = nullptr;
     }
+    if (g_state.ctx && g_state.out) pbig2_set_pair_output(g_state.ctx, nullptr, 0);
+    if (g_state.out) pbig2_host_free(g_state.out);
+    g_state.out = nullptr;
+    g_state.out_cap = 0;
     if (g_state.ctx) pbig2_destroy(g_state.ctx);
     g_state.ctx = nullptr;
 }
@@ -79,6 +100,7 @@ void pbig_init(unsigned int num, unsigned int range, unsigned int cs, unsigned i
     }
     for (auto& c : g_state.chunk)
         if (pbig2_host_alloc(kChunkPairs * 8, (void**)&c) != PBIG2_OK) die("pbig_init");
+    set_out(kChunkPairs);
 }
 
 void pbig_check(struct RectInfo* input, struct report* r) {
@@ -96,6 +118,13 @@ void pbig_check(struct RectInfo* input, struct report* r) {
         die("pbig_check");
     }
     if (np == 0) return;
+    const uint32_t* res = nullptr;
+    uint64_t rn = 0;
+    if (pbig2_result_pairs(g_state.ctx, &res, &rn) != PBIG2_OK) die("pbig_check");
+    if (res == g_state.out) {  // already in host memory
+        for (uint64_t k = 0; k < np; k++) (*r)(res[2 * k], res[2 * k + 1]);
+        return;
+    }
     uint64_t first = 0;
     int cur = 0;
     uint64_t cnt = np < kChunkPairs ? np : kChunkPairs;
@@ -114,4 +143,5 @@ void pbig_check(struct RectInfo* input, struct report* r) {
         cnt = ncnt;
         cur ^= 1;
     }
+    set_out(np + np / 4);  // the next query's pairs go straight to the host
 }

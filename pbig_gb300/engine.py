@@ -26,6 +26,7 @@ AUTO = 0xFFFFFFFF
 EXPORTS = [
     "pbig2_create", "pbig2_destroy", "pbig2_last_error", "pbig2_version", "pbig2_self_intersect",
     "pbig2_bipartite_intersect", "pbig2_batch_intersect", "pbig2_result_pairs", "pbig2_copy_pairs",
+    "pbig2_set_pair_output",
     "pbig2_result_scene_offsets", "pbig2_copy_pairs_async", "pbig2_sync", "pbig2_host_alloc",
     "pbig2_host_free", "pbig2_get_stats", "pbig2_tune_shift", "pbig2_self_intersect_noalloc",
     "pbig2_noalloc_last_error", "pbig2_set_option",
@@ -73,6 +74,7 @@ def lib():
         L.pbig2_copy_pairs.argtypes = [vp, vp, u64, u64, C.c_int, vp]
         L.pbig2_copy_pairs_async.argtypes = [vp, vp, u64, u64, C.c_int, vp]
         L.pbig2_sync.argtypes = [vp, vp]
+        L.pbig2_set_pair_output.argtypes = [vp, vp, u64]
         L.pbig2_result_scene_offsets.argtypes = [vp, C.POINTER(u64), u32]
         L.pbig2_get_stats.argtypes = [vp, C.POINTER(Stats)]
         L.pbig2_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
@@ -126,6 +128,7 @@ class Engine:
         self.device = device
         self.last_rc = OK
         self._keep = None
+        self._out = None
 
     def close(self):
         if getattr(self, "_ctx", None):
@@ -218,6 +221,24 @@ class Engine:
         else:
             ptr, loc, count = dst.data_ptr(), (DEVICE if dst.is_cuda else HOST), dst.shape[0]
         _check(self._L.pbig2_copy_pairs_async(self._ctx, C.c_void_p(ptr), first, count, loc, self._stream(stream)))
+
+    def set_pair_output(self, dst) -> None:
+        """Later self/bipartite queries store their pairs straight into dst
+        (a page-locked host or a device tensor [cap,2] of 4-byte elements);
+        None restores the context's own buffer. A result larger than dst is
+        redone into the context's buffer (``result_in(dst)`` tells)."""
+        if dst is None:
+            _check(self._L.pbig2_set_pair_output(self._ctx, None, 0))
+            self._out = None
+            return
+        if dst.dim() != 2 or dst.shape[1] != 2 or dst.element_size() != 4 or not dst.is_contiguous():
+            raise ValueError("pair output must be a contiguous [cap,2] tensor of 4-byte elements")
+        _check(self._L.pbig2_set_pair_output(self._ctx, C.c_void_p(dst.data_ptr()), dst.shape[0]))
+        self._out = dst
+
+    def result_in(self, dst) -> bool:
+        """True when the last result's pairs are in dst (set_pair_output)."""
+        return dst is not None and self.device_pairs()[0] == dst.data_ptr()
 
     def sync(self, stream=None):
         _check(self._L.pbig2_sync(self._ctx, self._stream(stream)))

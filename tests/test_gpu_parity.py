@@ -150,6 +150,42 @@ def test_repeated_queries_are_stable(engine):
         assert np.array_equal(canon(engine.pairs()), pa)
 
 
+def test_direct_pair_output(engine):
+    """Pairs stored straight into a caller's page-locked host buffer (or a
+    device buffer) equal the default path; a buffer that is too small makes
+    the engine redo the query into its own buffer; pageable host memory is
+    refused."""
+    import torch
+    boxes = gen.clustered3d(300000, seed=5)
+    n = engine.self_intersect(boxes, gen.RANGE)
+    want = canon(engine.pairs())
+    out = torch.empty((n + 100, 2), dtype=torch.int32).pin_memory()
+    try:
+        engine.set_pair_output(out)
+        assert engine.self_intersect(boxes, gen.RANGE) == n
+        assert engine.result_in(out)
+        assert np.array_equal(canon(out[:n].numpy().view(np.uint32)), want)
+        assert np.array_equal(canon(engine.pairs()), want)
+        small = torch.empty((n // 2, 2), dtype=torch.int32).pin_memory()
+        engine.set_pair_output(small)
+        assert engine.self_intersect(boxes, gen.RANGE) == n
+        assert not engine.result_in(small)
+        assert np.array_equal(canon(engine.pairs()), want)
+        dev = torch.empty((n + 1, 2), dtype=torch.int32, device="cuda")
+        engine.set_pair_output(dev)
+        assert engine.self_intersect(to_device(boxes), gen.RANGE) == n
+        assert engine.result_in(dev)
+        assert np.array_equal(canon(dev[:n].cpu().numpy().view(np.uint32)), want)
+        red, blue = gen.mixed3d(100000, seed=0), gen.mixed3d(100000, seed=1)
+        nb = engine.bipartite_intersect(red, blue, gen.RANGE)
+        assert engine.result_in(dev) and np.array_equal(dev[:nb].cpu().numpy().view(np.uint32), engine.pairs())
+        with pytest.raises(PbigError):
+            engine.set_pair_output(torch.empty((16, 2), dtype=torch.int32))
+    finally:
+        engine.set_pair_output(None)
+    assert engine.self_intersect(boxes, gen.RANGE) == n and not engine.result_in(out)
+
+
 def test_output_capacity_growth(engine):
     """A tiny scene first (small buffers), then one with millions of pairs:
     the pair buffer must grow and the count stay exact."""
