@@ -71,6 +71,15 @@ typedef struct {
      * pair kernels), grouping by scene, and within the pair test: the
      * small-cell, medium-cell and block kernels */
     double phase_ms[9];
+    /* the reference's own work statistics for the same grid (sched_phase,
+     * src/pbig/pbig.cu:1586-1688): numCompPairs = sum of n*n/2, jobs = sum
+     * of ceil(n/256), over the cells -- or merged blocks -- of n >= 2 boxes;
+     * max_cell = the largest of them; merged_blocks = merged blocks of two
+     * or more cells (merged mode) */
+    uint64_t comp_pairs;
+    uint64_t jobs;
+    uint32_t max_cell;
+    uint32_t merged_blocks;
 } pbig2_stats;
 
 /* Context: one device, owns its buffers and streams. Not thread-safe; use
@@ -154,6 +163,14 @@ PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
  * CUDA graph once, and replay it for later batches with the same box buffer,
  * dims, range and no more boxes, cells or scenes than the captured one. */
 #define PBIG2_OPT_GRAPH 1
+/* PBIG2_OPT_MERGED (default 0): the reference's MERGED=1 build. After the
+ * count, sparse neighbouring cells are merged greedily into blocks of at
+ * most 256 box entries (h_merge_grids, src/pbig/pbig.cu:1066-1251; on the
+ * host, as there), every box enters a block once at the minimum corner of
+ * (box range x block) (d_postcounting, :223-318), and the pair test runs per
+ * block. The pair set is the same; the work statistics (pbig2_stats) are
+ * the merged build's. Self and red/blue queries only. */
+#define PBIG2_OPT_MERGED 2
 PBIG2_API int pbig2_set_option(pbig2_ctx* ctx, int option, int64_t value);
 
 /* Allocation-free self-intersection (no counterpart in the reference).

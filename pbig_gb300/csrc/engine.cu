@@ -337,6 +337,10 @@ static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t nc
     s.cells = ncells;
     s.entries = h.entries;
     s.pair_tests = h.tests;
+    s.comp_pairs = h.comp_pairs;
+    s.jobs = h.jobs;
+    s.max_cell = h.max_cell ? h.max_cell : (h.entries ? 1u : 0u);
+    s.merged_blocks = c->merged_blocks;
     s.pairs = h.pairs;
     s.cell_shift = scenes.empty() ? 0 : scenes[0].shift;
     s.scenes = nsc;
@@ -390,6 +394,71 @@ static int capture_graph(pbig2_ctx* c, const Params& p0, const uint32_t* d_boxes
     G.launches = 12;  // count, scan (3), expand, scatter, pairs (3), scene grouping (3)
     G.buffers = c->buffers_sig();
     return PBIG2_OK;
+}
+
+// Merged mode, the reference's h_merge_grids (src/pbig/pbig.cu:1066-1251) on
+// the counts of a first pass: cells in id order; a cell that is in no block
+// grows a block from itself along +x, +y (and +z), one slab at a time, while
+// the new slab holds no merged cell and the block's running count (the sum of
+// the first pass's per-cell counts) stays <= 256. merged[c] = the block root
+// of every cell of a block of two or more cells (the root included), else
+// kUnmerged. Returns the number of such blocks.
+static uint32_t merge_cells(std::vector<uint32_t>& nrs, std::vector<uint32_t>& merged, uint32_t nrc, int dims) {
+    const uint64_t C = nrs.size();
+    const uint32_t kLimit = 256;  // NTPB of the shipped build
+    merged.assign(C, kUnmerged);
+    const uint64_t nrc2 = (uint64_t)nrc * nrc;
+    uint32_t blocks = 0;
+    // try to add the slab next to block (root, h x v x u) along axis dir
+    auto grow = [&](uint64_t root, int dir, uint32_t& h, uint32_t& v, uint32_t& u) -> int {
+        uint64_t step1, step2, n1, n2, base;
+        if (dims == 2) {
+            step1 = 0;
+            n1 = 1;
+            step2 = dir == 0 ? nrc : 1;
+            n2 = dir == 0 ? v : h;
+            base = dir == 0 ? root + h : root + (uint64_t)v * nrc;
+        } else if (dir == 0) {
+            step1 = nrc2; step2 = nrc; n1 = u; n2 = v; base = root + h;
+        } else if (dir == 1) {
+            step1 = nrc2; step2 = 1; n1 = u; n2 = h; base = root + (uint64_t)v * nrc;
+        } else {
+            step1 = nrc; step2 = 1; n1 = v; n2 = h; base = root + (uint64_t)u * nrc2;
+        }
+        for (uint64_t a = 0; a < n1; a++)
+            for (uint64_t b = 0; b < n2; b++)
+                if (merged[base + a * step1 + b * step2] != kUnmerged) return 0;
+        uint64_t acc = nrs[root];
+        for (uint64_t a = 0; a < n1; a++)
+            for (uint64_t b = 0; b < n2; b++) {
+                acc += nrs[base + a * step1 + b * step2];
+                if (acc > kLimit) return 0;
+            }
+        for (uint64_t a = 0; a < n1; a++)
+            for (uint64_t b = 0; b < n2; b++) merged[base + a * step1 + b * step2] = (uint32_t)root;
+        merged[root] = (uint32_t)root;
+        nrs[root] = (uint32_t)acc;
+        if (dir == 0) h++;
+        else if (dir == 1) v++;
+        else u++;
+        return 1;
+    };
+    for (uint64_t i = 0; i < C; i++) {
+        if (merged[i] != kUnmerged) continue;
+        const uint64_t gx = i % nrc;
+        const uint64_t gy = dims == 3 ? (i % nrc2) / nrc : i / nrc;
+        const uint64_t gz = dims == 3 ? i / nrc2 : 0;
+        uint32_t h = 1, v = 1, u = 1;
+        int progress;
+        do {
+            progress = 0;
+            if (gx + h < nrc) progress += grow(i, 0, h, v, u);
+            if (gy + v < nrc) progress += grow(i, 1, h, v, u);
+            if (dims == 3 && gz + u < nrc) progress += grow(i, 2, h, v, u);
+        } while (progress != 0);
+        if (merged[i] == (uint32_t)i) blocks++;
+    }
+    return blocks;
 }
 
 static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, int dims, uint32_t range,
@@ -505,6 +574,25 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     p.tile_state = c->d_state.as<unsigned long long>();
     p.ctr = c->d_ctr.as<Ctr>();
     p.dyn = nullptr;
+    c->merged_blocks = 0;
+    bool one_grid = true;  // a single scene, or red and blue sharing one grid
+    for (uint32_t i = 0; i < nsc; i++) one_grid = one_grid && scenes[i].grid_of == 0;
+    if (c->merged_mode && one_grid && !grouped) {
+        // first pass: plain counts; merge on the host; the pass below then
+        // counts, bins and tests per merged block
+        Params p0 = p;
+        p0.counts = c->d_counts.as<uint32_t>();
+        CK(cudaMemsetAsync(p.ctr, 0, sizeof(Ctr), st));
+        CK(launch_count(p0, dims, st));
+        std::vector<uint32_t> nrs(ncells), merged;
+        CK(cudaMemcpyAsync(nrs.data(), p0.counts, ncells * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        c->merged_blocks = merge_cells(nrs, merged, tab[0].nrc, dims);
+        CK(c->d_merged.ensure(ncells * 4, false, st));
+        CK(cudaMemcpyAsync(c->d_merged.p, merged.data(), ncells * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));  // `merged` goes out of scope
+        p.merged = c->d_merged.as<uint32_t>();
+    }
     bool need_full = true;
     // self/bipartite pairs go straight to the caller's buffer when one is set;
     // a result that does not fit is redone into the context's buffer
@@ -906,6 +994,10 @@ PBIG2_API int pbig2_set_option(pbig2_ctx* c, int option, int64_t value) {
     if (option == PBIG2_OPT_GRAPH) {
         c->use_graph = value != 0;
         if (!c->use_graph) c->drop_graph();
+        return PBIG2_OK;
+    }
+    if (option == PBIG2_OPT_MERGED) {
+        c->merged_mode = value != 0;
         return PBIG2_OK;
     }
     return fail(PBIG2_EINVAL, "unknown option %d", option);

@@ -51,6 +51,9 @@ struct pbig2_ctx {
     cudaStream_t own_stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t evp[9] = {};
+    pbig::DevBuf d_merged;  // merged mode: cell -> root table
+    bool merged_mode = false;
+    uint32_t merged_blocks = 0;  // merged blocks of the last query
     pbig::DevBuf d_boxes, d_counts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
         d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims;
     pbig::HostPinned h_ctr, h_stage;

@@ -89,7 +89,7 @@ __device__ __forceinline__ void stage_boxes(const Params& p, uint64_t b0, uint32
     }
 }
 
-template <int D, bool SCATTER>
+template <int D, bool SCATTER, bool MERGED>
 __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t* sbox, uint64_t b0,
                                                 uint32_t nb) {
     constexpr uint32_t W = 2 * D + 1;
@@ -149,9 +149,30 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
             const uint32_t lq = q - o_excl;
             const uint32_t i = lq % o_sx, rr = lq / o_sx;
             const uint32_t j = rr % o_sy, k = rr / o_sy;
-            const uint64_t gid = o_base + ((uint64_t)k * o_nrc + j) * o_nrc + i;
-            if (SCATTER) {
-                const uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
+            uint64_t gid = o_base + ((uint64_t)k * o_nrc + j) * o_nrc + i;
+            uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
+            bool take = true;
+            if (MERGED) {
+                // merged mode: a cell of a merged block stands for the block's
+                // root, and a box enters the block once, at the minimum corner of
+                // (box range x block) -- the first-visit rule of d_postcounting,
+                // pbig.cu:223-318; "starts here" is then per axis "the box's
+                // first cell is inside the block"
+                const uint32_t m = p.merged[gid];
+                if (m != kUnmerged) {
+                    const uint64_t nr = o_nrc;
+                    const uint32_t ci = (uint32_t)(gid % nr), cj = (uint32_t)((gid / nr) % nr);
+                    const uint32_t ck = D == 3 ? (uint32_t)(gid / (nr * nr)) : 0u;
+                    const uint32_t lx = ci - i, ly = cj - j, lz = ck - k;
+                    const uint32_t rx = (uint32_t)(m % nr), ry = (uint32_t)((m / nr) % nr);
+                    const uint32_t rz = D == 3 ? (uint32_t)(m / (nr * nr)) : 0u;
+                    take = ci == max(lx, rx) && cj == max(ly, ry) && ck == max(lz, rz);
+                    gid = m;
+                    f = (lx >= rx ? 1u : 0u) | (ly >= ry ? 2u : 0u) | ((D == 2 || lz >= rz) ? 4u : 0u);
+                }
+            }
+            if (!take) {
+            } else if (SCATTER) {
                 // after the scan a cell's counter holds its end: counting it
                 // down hands out the cell's slots (and leaves its start)
                 const uint64_t pos = (uint64_t)(atomicSub(&p.counts[gid], 1u) - 1u);
@@ -174,7 +195,7 @@ __global__ void k_zero_counts(Params pin) {
     for (uint64_t i = 4 * n4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.ncells; i += stride) p.counts[i] = 0;
 }
 
-template <int D>
+template <int D, bool MERGED>
 __global__ void __launch_bounds__(kBoxThreads) k_count(Params pin) {
     __shared__ __align__(16) uint32_t sbox[kBoxThreads * (2 * D + 1)];
     const Params p = resolve(pin);
@@ -182,12 +203,12 @@ __global__ void __launch_bounds__(kBoxThreads) k_count(Params pin) {
         const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
         stage_boxes<D>(p, b0, nb, sbox);
         __syncthreads();
-        enumerate_cells<D, false>(p, sbox, b0, nb);
+        enumerate_cells<D, false, MERGED>(p, sbox, b0, nb);
         __syncthreads();
     }
 }
 
-template <int D>
+template <int D, bool MERGED>
 __global__ void __launch_bounds__(kBoxThreads) k_scatter(Params pin) {
     __shared__ __align__(16) uint32_t sbox[kBoxThreads * (2 * D + 1)];
     const Params p = resolve(pin);
@@ -195,7 +216,7 @@ __global__ void __launch_bounds__(kBoxThreads) k_scatter(Params pin) {
         const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
         stage_boxes<D>(p, b0, nb, sbox);
         __syncthreads();
-        enumerate_cells<D, true>(p, sbox, b0, nb);
+        enumerate_cells<D, true, MERGED>(p, sbox, b0, nb);
         __syncthreads();
     }
 }
@@ -236,7 +257,9 @@ struct TileRec {                         // 64 bytes per tile
     unsigned long long sum;              // entries; exclusive prefix after k_scan_prefix
     unsigned long long tests;            // pair tests of the tile's cells
     uint32_t chunk[kScanChunks];         // entries per chunk
-    uint32_t pad[4];
+    unsigned long long comp;             // sum of n*n/2 over the tile's cells of n >= 2
+    uint32_t jobs;                       // sum of ceil(n/256) over them
+    uint32_t maxc;                       // largest of them
 };
 static_assert(sizeof(TileRec) == 64, "tile record layout");
 
@@ -291,12 +314,27 @@ __device__ __forceinline__ void reduce_chunk(TileRec* rec, uint64_t ch, const ui
         if (lsum) atomicAdd(&r.sum, (unsigned long long)lsum);
     }
     if (__any_sync(FULL_MASK, big != 0)) {
-        unsigned long long tests = 0;
+        unsigned long long tests = 0, comp = 0;
+        uint32_t jobs = 0, maxc = 0;
 #pragma unroll
-        for (int k = 0; k < kScanPerThread; k++)
-            if (v[k] >= 2u) tests += (unsigned long long)v[k] * (v[k] - 1u) / 2u;
+        for (int k = 0; k < kScanPerThread; k++) {
+            if (v[k] >= 2u) {
+                tests += (unsigned long long)v[k] * (v[k] - 1u) / 2u;
+                comp += (unsigned long long)v[k] * v[k] / 2u;
+                jobs += (v[k] + 255u) >> 8;
+                maxc = max(maxc, v[k]);
+            }
+        }
         tests = warp_sum_u64(tests);
-        if (lane == 0 && tests) atomicAdd(&r.tests, tests);
+        comp = warp_sum_u64(comp);
+        jobs = __reduce_add_sync(FULL_MASK, jobs);
+        maxc = __reduce_max_sync(FULL_MASK, maxc);
+        if (lane == 0 && tests) {
+            atomicAdd(&r.tests, tests);
+            atomicAdd(&r.comp, comp);
+            atomicAdd(&r.jobs, jobs);
+            atomicMax(&r.maxc, maxc);
+        }
     }
 }
 
@@ -318,35 +356,47 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_scan_reduce(Params pin) {
 
 constexpr int kPrefixThreads = 1024;
 __global__ void __launch_bounds__(kPrefixThreads) k_scan_prefix(Params pin) {
-    __shared__ unsigned long long s_part[kPrefixThreads / 32][2];
-    __shared__ unsigned long long s_carry[2];
+    __shared__ unsigned long long s_part[kPrefixThreads / 32][4];
+    __shared__ unsigned long long s_carry[4];
     const Params p = resolve(pin);
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const uint64_t tiles = (p.ncells + kScanTile - 1) / kScanTile;
     TileRec* rec = reinterpret_cast<TileRec*>(p.tile_state);
-    if (t == 0) s_carry[0] = s_carry[1] = 0;
+    if (t == 0) s_carry[0] = s_carry[1] = s_carry[2] = s_carry[3] = 0;
     // rounds of 4 tiles per thread: all loads of a round in flight together
     for (uint64_t r0 = 0; r0 < tiles; r0 += 4 * kPrefixThreads) {
-        unsigned long long x[4], y[4], sx = 0, sy = 0;
+        unsigned long long x[4], sx = 0, sy = 0, sc = 0, sj = 0, sm = 0;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const uint64_t i = r0 + 4 * (uint64_t)t + k;
             x[k] = i < tiles ? rec[i].sum : 0ull;
-            y[k] = i < tiles ? rec[i].tests : 0ull;
             sx += x[k];
-            sy += y[k];
+            if (i < tiles) {
+                sy += rec[i].tests;
+                sc += rec[i].comp;
+                sj += rec[i].jobs;
+                sm = max(sm, (unsigned long long)rec[i].maxc);
+            }
         }
         const unsigned long long ix = warp_incl_scan64(sx);
-        const unsigned long long iy = warp_sum_u64(sy);
+        const unsigned long long iy = warp_sum_u64(sy), ic = warp_sum_u64(sc), ij = warp_sum_u64(sj);
+        const unsigned long long im = __reduce_max_sync(FULL_MASK, (uint32_t)sm);
         if (lane == 31) s_part[warp][0] = ix;
-        if (lane == 0) s_part[warp][1] = iy;
+        if (lane == 0) {
+            s_part[warp][1] = iy;
+            s_part[warp][2] = ic;
+            s_part[warp][3] = (ij << 32) | im;  // jobs < 2^32, max < 2^32
+        }
         __syncthreads();
-        unsigned long long wo = s_carry[0], tot = 0, tt = 0;
+        unsigned long long wo = s_carry[0], tot = 0, tt = 0, tc = 0, tj = 0, tm = 0;
         for (int w = 0; w < kPrefixThreads / 32; w++) {
             const unsigned long long a = s_part[w][0];
             if (w < (int)warp) wo += a;
             tot += a;
             tt += s_part[w][1];
+            tc += s_part[w][2];
+            tj += s_part[w][3] >> 32;
+            tm = max(tm, s_part[w][3] & 0xffffffffull);
         }
         unsigned long long run = wo + (ix - sx);
 #pragma unroll
@@ -359,6 +409,8 @@ __global__ void __launch_bounds__(kPrefixThreads) k_scan_prefix(Params pin) {
         if (t == 0) {
             s_carry[0] += tot;
             s_carry[1] += tt;
+            s_carry[2] += tc;
+            s_carry[3] = ((s_carry[3] >> 32) + tj) << 32 | max(s_carry[3] & 0xffffffffull, tm);
         }
         __syncthreads();
     }
@@ -366,6 +418,9 @@ __global__ void __launch_bounds__(kPrefixThreads) k_scan_prefix(Params pin) {
         const unsigned long long total = s_carry[0];
         p.ctr->entries = total;
         p.ctr->tests = s_carry[1];
+        p.ctr->comp_pairs = s_carry[2];
+        p.ctr->jobs = s_carry[3] >> 32;
+        p.ctr->max_cell = (uint32_t)(s_carry[3] & 0xffffffffull);
         if (total >= (1ull << 32)) atomicOr(&p.ctr->err, kErrEntryOvf);
     }
 }
@@ -1401,16 +1456,26 @@ cudaError_t launch_count(const Params& p, int dims, cudaStream_t st) {
     k_zero_counts<<<(unsigned)((g_sm_count > 0 ? g_sm_count : 152) * 4), 512, 0, st>>>(p);
     const unsigned g = box_grid(p.nboxes);
     if (g == 0) return cudaSuccess;
-    if (dims == 2) k_count<2><<<g, kBoxThreads, 0, st>>>(p);
-    else k_count<3><<<g, kBoxThreads, 0, st>>>(p);
+    if (p.merged) {
+        if (dims == 2) k_count<2, true><<<g, kBoxThreads, 0, st>>>(p);
+        else k_count<3, true><<<g, kBoxThreads, 0, st>>>(p);
+    } else {
+        if (dims == 2) k_count<2, false><<<g, kBoxThreads, 0, st>>>(p);
+        else k_count<3, false><<<g, kBoxThreads, 0, st>>>(p);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st) {
     const unsigned g = box_grid(p.nboxes);
     if (g == 0) return cudaSuccess;
-    if (dims == 2) k_scatter<2><<<g, kBoxThreads, 0, st>>>(p);
-    else k_scatter<3><<<g, kBoxThreads, 0, st>>>(p);
+    if (p.merged) {
+        if (dims == 2) k_scatter<2, true><<<g, kBoxThreads, 0, st>>>(p);
+        else k_scatter<3, true><<<g, kBoxThreads, 0, st>>>(p);
+    } else {
+        if (dims == 2) k_scatter<2, false><<<g, kBoxThreads, 0, st>>>(p);
+        else k_scatter<3, false><<<g, kBoxThreads, 0, st>>>(p);
+    }
     return cudaGetLastError();
 }
 

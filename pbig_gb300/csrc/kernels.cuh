@@ -50,10 +50,12 @@ struct Ctr {
     unsigned int n_list[kNumLists];     // class list sizes
     unsigned int n_tasks;               // tile tasks written for huge cells
     unsigned int need_tasks;            // tile tasks needed
-    unsigned int pad;
+    unsigned int max_cell;              // largest cell (or merged block) of two or more boxes
     unsigned long long entries;         // E
     unsigned long long pairs;           // pairs found (may exceed capacity)
     unsigned long long tests;           // sum of n(n-1)/2 over cells
+    unsigned long long comp_pairs;      // sum of n*n/2 over cells of n >= 2 (the reference's numCompPairs)
+    unsigned long long jobs;            // sum of ceil(n/256) over cells of n >= 2 (its 256-row jobs)
 };
 
 // query sizes read from device memory (graph replays: one captured graph
@@ -87,7 +89,10 @@ struct Params {
     uint64_t out_cap;
     Ctr* ctr;
     const RunDims* dyn;           // when set, overrides nboxes / ncells / nscenes
+    const uint32_t* merged;       // merged mode (one scene): cell -> root of its merged block, or kUnmerged
 };
+
+constexpr uint32_t kUnmerged = 0x0fffff11u;  // a cell outside every merged block
 
 // launchers (all asynchronous on `st`); dims is 2 or 3
 // grids: sized from p.nboxes / p.ncells (which must then be upper bounds

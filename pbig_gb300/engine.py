@@ -43,7 +43,9 @@ class Stats(C.Structure):
     _fields_ = [("boxes", C.c_uint64), ("bad_boxes", C.c_uint64), ("cells", C.c_uint64),
                 ("entries", C.c_uint64), ("pair_tests", C.c_uint64), ("pairs", C.c_uint64),
                 ("cell_shift", C.c_uint32), ("scenes", C.c_uint32), ("kernels", C.c_uint32),
-                ("reserved", C.c_uint32), ("device_ms", C.c_double), ("phase_ms", C.c_double * 9)]
+                ("reserved", C.c_uint32), ("device_ms", C.c_double), ("phase_ms", C.c_double * 9),
+                ("comp_pairs", C.c_uint64), ("jobs", C.c_uint64), ("max_cell", C.c_uint32),
+                ("merged_blocks", C.c_uint32)]
 
     PHASES = ("count", "scan", "expand", "scatter", "pairs", "group", "pairs_small", "pairs_med", "pairs_block")
 
@@ -252,6 +254,12 @@ class Engine:
 
     def result_count(self) -> int:
         return self.device_pairs()[1]
+
+    def set_merged(self, on: bool) -> None:
+        """The reference's MERGED=1 build: sparse cells merged into blocks of
+        at most 256 entries, pairs tested per block (same pair set, the merged
+        build's work statistics)."""
+        _check(self._L.pbig2_set_option(self._ctx, 2, int(bool(on))))
 
     def set_graphs(self, on: bool) -> None:
         """Capture/replay batched queries as CUDA graphs (on by default)."""
