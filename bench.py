@@ -211,9 +211,9 @@ def run_reference(args, rank, ws):
     if rank != 0:
         return
     from oracle import oracle as O
-    if args.workload == "serving":
-        print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving mode (one pbig_check "
-                          "at a time on a process-global state)"}), flush=True)
+    if args.workload in ("serving", "update4m"):
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving mode or resident scenes "
+                          "(one pbig_check at a time, from scratch, on a process-global state)"}), flush=True)
         return
     if args.workload == "batched":
         return run_reference_batched(args)
@@ -479,6 +479,87 @@ def run_batched(args, rank, local, ws):
     eng.close()
 
 
+def run_update(args, rank, local, ws):
+    """Incremental updates of a resident scene (pbig2_scene_*): the clustered
+    4M-box scene stays on the device, every step moves 1% of its boxes by
+    N(0, 0.001) and asks for the pairs they had and have (copied to the host)
+    and the updated full pair list (kept on the device). The same boxes are
+    also queried from scratch for comparison."""
+    import torch
+    from pbig_gb300 import Engine, Scene, gen
+    from pbig_gb300.serve import move_indices
+
+    torch.cuda.set_device(local)
+    boxes = gen.clustered3d(4194304, seed=0)
+    n = len(boxes)
+    eng = Engine(local)
+    sc = Scene(eng, boxes, gen.RANGE, keep_pairs=not args.delta_only)
+    cur = boxes.copy()
+    steps = []
+
+    def pinned(a):  # page-locked copy of a host array
+        t = torch.empty(a.shape, dtype=torch.int32).pin_memory()
+        v = t.numpy().view(np.uint32)
+        v[...] = a
+        return v
+
+    for i in range(args.warmup + args.steps):  # the moves, made before the timing (page-locked inputs)
+        idx = move_indices(n, 0.01, 7000 + i)
+        gen.move3d(cur, idx, 7000 + i, sigma=0.001)
+        steps.append((pinned(idx), pinned(cur[idx])))
+    out_rem = pinned(np.zeros((4 << 20, 2), dtype=np.uint32))
+    out_add = pinned(np.zeros((4 << 20, 2), dtype=np.uint32))
+    for idx, nb in steps[:args.warmup]:
+        sc.move(idx, nb)
+        sc.delta(out_rem, out_add)
+    ts, moved, delta_pairs = [], 0, 0
+    with ClockSampler(local) as clk:
+        for idx, nb in steps[args.warmup:]:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            nr, na = sc.move(idx, nb)
+            rem, add = sc.delta(out_rem, out_add)
+            ts.append(time.perf_counter() - t0)
+            moved += len(idx)
+            delta_pairs += nr + na
+    t_up = allmax(float(np.mean(ts)), ws)
+    P = len(sc.pairs()) if not args.delta_only else None
+    # the same final boxes from scratch, device-resident
+    dev = torch.from_numpy(cur.view(np.int32)).to(f"cuda:{local}")
+    for _ in range(2):
+        eng.self_intersect(dev, gen.RANGE)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        P2 = eng.self_intersect(dev, gen.RANGE)
+        assert P is None or P2 == P
+    P = P2
+    torch.cuda.synchronize()
+    t_full = (time.perf_counter() - t0) / reps
+    line = {
+        "metric": METRIC, "value": n * ws / t_up, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_up * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "incremental updates of a resident scene: 4,194,304 clustered 3D boxes (seed 0), "
+                               "each step moves 1% of them (41,943 boxes) by N(0,0.001); value = scene boxes / update time"
+                               + ("; delta only (no full pair list kept)" if args.delta_only else
+                                  "; the full pair list is kept current on the device"),
+                   "pairs": P, "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "moved_per_step": moved // max(1, args.steps), "delta_pairs_per_step": delta_pairs // max(1, args.steps),
+        "full_query_ms": t_full * 1e3, "speedup_vs_full_query": t_full / t_up,
+        "e2e": {"value": n * ws / t_up, "unit": UNIT, "h2d_bytes_per_step": int(moved // max(1, args.steps) * 32),
+                "d2h_bytes_per_step": int(delta_pairs // max(1, args.steps) * 8),
+                "note": "moved rows go up from the host and both pair lists come back inside the timed step"},
+        "gpu_launches": 9 * args.steps,  # per move: check, mark, query, remove, write, insert, query, filter, unmark
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sc.close()
+    eng.close()
+
+
 def run_serving(args, rank, local, ws):
     """Serving loop: Poisson arrivals of scene queries (sizes log-uniform in
     [1024, 1048576], the batched scenes' generator) and updates (30 %: 1 % of
@@ -539,6 +620,7 @@ def main():
     ap.add_argument("--scenes", type=int, default=4096, help="scenes of the batched workload")
     ap.add_argument("--duration", type=float, default=1.0, help="seconds of arrivals (serving workload)")
     ap.add_argument("--rate", type=float, default=2000.0, help="arrivals per second (serving workload)")
+    ap.add_argument("--delta-only", action="store_true", help="update workload: keep no full pair list")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -549,6 +631,8 @@ def main():
         run_batched(args, rank, local, ws)
     elif args.workload == "serving":
         run_serving(args, rank, local, ws)
+    elif args.workload == "update4m":
+        run_update(args, rank, local, ws)
     else:
         run_gb300(args, rank, local, ws)
     if ws > 1:

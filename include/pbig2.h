@@ -192,6 +192,37 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
                                            uint64_t* npairs, void* stream);
 PBIG2_API const char* pbig2_noalloc_last_error(void);
 
+/* Resident scenes and incremental updates (no counterpart in the reference,
+ * which re-runs pbig_check from scratch). pbig2_scene_create runs the full
+ * self-intersection of n boxes on ctx (autotuned when cell_shift is
+ * PBIG2_AUTO; every box must be valid) and keeps the boxes, a grid with
+ * slack in every cell and the full pair list on the device; *npairs gets the
+ * pair count. pbig2_scene_move gives k boxes new coordinates (idx: their
+ * indices, distinct; new_boxes: k RectInfo records with rid = the index,
+ * host or device memory) and re-bins only those boxes. *n_removed gets the
+ * number of pairs the moved boxes had before the move, *n_added the number
+ * they have after it (pbig2_scene_delta: both lists, device memory, a pair
+ * of two moved boxes once); the full list (pbig2_scene_pairs) becomes the
+ * old list without the removed pairs plus the added ones -- an O(pairs)
+ * step that flags = PBIG2_SCENE_DELTA_ONLY leaves out. The scene uses
+ * ctx's stream and buffers: one scene call at a time per context, and the
+ * context's last-result pointers are overwritten by pbig2_scene_create. */
+typedef struct pbig2_scene pbig2_scene;
+#define PBIG2_SCENE_DELTA_ONLY 1u /* flags: moves report their delta only; no full list is kept */
+PBIG2_API int pbig2_scene_create(pbig2_ctx* ctx, const uint32_t* boxes, uint64_t n, uint32_t dims, uint32_t range,
+                                 uint32_t cell_shift, int boxes_loc, uint32_t flags, pbig2_scene** scene,
+                                 uint64_t* npairs);
+PBIG2_API int pbig2_scene_destroy(pbig2_scene* scene);
+PBIG2_API int pbig2_scene_move(pbig2_scene* scene, const uint32_t* idx, uint64_t k, const uint32_t* new_boxes,
+                               int boxes_loc, uint64_t* n_removed, uint64_t* n_added);
+PBIG2_API int pbig2_scene_delta(pbig2_scene* scene, const uint32_t** removed, uint64_t* n_removed,
+                                const uint32_t** added, uint64_t* n_added);
+PBIG2_API int pbig2_scene_pairs(pbig2_scene* scene, const uint32_t** pairs, uint64_t* npairs);
+PBIG2_API int pbig2_scene_boxes(pbig2_scene* scene, const uint32_t** boxes, uint64_t* n);
+/* Copy the first count pairs of the full list (which = 0), the removed
+ * (1) or the added (2) pairs of the last move into dst (host or device). */
+PBIG2_API int pbig2_scene_copy(pbig2_scene* scene, int which, uint32_t* dst, uint64_t count);
+
 /* Cell-size autotuner: the shift the engine would pick for these boxes
  * (host memory), from a sample of at most `sample` boxes. */
 PBIG2_API int pbig2_tune_shift(const uint32_t* boxes, uint64_t n, uint32_t dims, uint32_t range,

@@ -30,6 +30,8 @@ static int fail(int code, const char* fmt, ...) {
     return code;
 }
 
+int api_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+
 #define CK(expr)                                                                                   \
     do {                                                                                           \
         cudaError_t _e = (expr);                                                                   \

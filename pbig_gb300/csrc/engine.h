@@ -42,6 +42,8 @@ TuneResult tune_shift_sample(const uint32_t* boxes, uint64_t n_avail, uint64_t n
                              uint64_t max_sample);
 TuneResult tune_shift_analytic(const uint32_t* sample, uint64_t nsample, uint64_t n, int dims, uint32_t range);
 uint32_t nrc_for(uint32_t range, uint32_t shift);
+// records `msg` as the calling thread's pbig2_last_error() and returns code
+int api_fail(int code, const char* msg);
 
 }  // namespace pbig
 

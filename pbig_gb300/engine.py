@@ -29,7 +29,8 @@ EXPORTS = [
     "pbig2_set_pair_output",
     "pbig2_result_scene_offsets", "pbig2_copy_pairs_async", "pbig2_sync", "pbig2_host_alloc",
     "pbig2_host_free", "pbig2_get_stats", "pbig2_tune_shift", "pbig2_self_intersect_noalloc",
-    "pbig2_noalloc_last_error", "pbig2_set_option",
+    "pbig2_noalloc_last_error", "pbig2_set_option", "pbig2_scene_create", "pbig2_scene_destroy",
+    "pbig2_scene_move", "pbig2_scene_delta", "pbig2_scene_pairs", "pbig2_scene_boxes", "pbig2_scene_copy",
 ]
 
 
@@ -77,6 +78,11 @@ def lib():
         L.pbig2_copy_pairs_async.argtypes = [vp, vp, u64, u64, C.c_int, vp]
         L.pbig2_sync.argtypes = [vp, vp]
         L.pbig2_set_pair_output.argtypes = [vp, vp, u64]
+        L.pbig2_scene_create.argtypes = [vp, vp, u64, u32, u32, u32, C.c_int, u32, C.POINTER(vp), C.POINTER(u64)]
+        L.pbig2_scene_destroy.argtypes = [vp]
+        L.pbig2_scene_move.argtypes = [vp, vp, u64, vp, C.c_int, C.POINTER(u64), C.POINTER(u64)]
+        L.pbig2_scene_copy.argtypes = [vp, C.c_int, vp, u64]
+        L.pbig2_scene_pairs.argtypes = [vp, C.POINTER(vp), C.POINTER(u64)]
         L.pbig2_result_scene_offsets.argtypes = [vp, C.POINTER(u64), u32]
         L.pbig2_get_stats.argtypes = [vp, C.POINTER(Stats)]
         L.pbig2_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
@@ -269,6 +275,71 @@ class Engine:
         s = Stats()
         _check(self._L.pbig2_get_stats(self._ctx, C.byref(s)))
         return s.as_dict()
+
+
+class Scene:
+    """A resident scene (pbig2_scene_*): boxes, a grid with slack and the
+    full pair list stay on the device; move() re-bins only the moved boxes
+    and reports the pairs they had before and have after the move."""
+
+    def __init__(self, engine: Engine, boxes: np.ndarray, range_: int, cell_shift: int | None = None,
+                 keep_pairs: bool = True):
+        self._L = engine._L
+        self._eng = engine  # the scene uses the engine's stream and buffers
+        ptr, n, dims, loc, keep = _boxes_arg(boxes)
+        self.dims = dims
+        sc = C.c_void_p()
+        out = C.c_uint64()
+        _check(self._L.pbig2_scene_create(engine._ctx, C.c_void_p(ptr), n, dims, range_,
+                                           AUTO if cell_shift is None else cell_shift, loc,
+                                           0 if keep_pairs else 1, C.byref(sc), C.byref(out)))
+        self._sc = sc
+        self.npairs = out.value
+        self.nremoved = self.nadded = 0
+
+    def move(self, idx, new_boxes) -> tuple[int, int]:
+        """Boxes idx get the coordinates of new_boxes (RectInfo rows whose rid
+        is the index); returns (pairs the moved boxes had, pairs they have)."""
+        idx = np.ascontiguousarray(idx, dtype=np.uint32)
+        nb = np.ascontiguousarray(new_boxes, dtype=np.uint32)
+        if nb.shape != (idx.shape[0], 2 * self.dims + 1):
+            raise ValueError("new_boxes must hold one RectInfo row per index")
+        r, a = C.c_uint64(), C.c_uint64()
+        _check(self._L.pbig2_scene_move(self._sc, C.c_void_p(idx.ctypes.data), idx.shape[0],
+                                        C.c_void_p(nb.ctypes.data), HOST, C.byref(r), C.byref(a)))
+        self.nremoved, self.nadded = r.value, a.value
+        return r.value, a.value
+
+    def _copy(self, which: int, count: int, out=None) -> np.ndarray:
+        if out is None:
+            out = np.empty((count, 2), dtype=np.uint32)
+        elif out.shape[0] < count or out.shape[1:] != (2,) or out.dtype.itemsize != 4 or not out.flags.c_contiguous:
+            raise ValueError("output array too small or not a contiguous [n,2] array of 4-byte elements")
+        _check(self._L.pbig2_scene_copy(self._sc, which, C.c_void_p(out.ctypes.data), count))
+        return out[:count]
+
+    def pairs(self) -> np.ndarray:
+        p = C.c_void_p()
+        n = C.c_uint64()
+        _check(self._L.pbig2_scene_pairs(self._sc, C.byref(p), C.byref(n)))
+        return self._copy(0, n.value)
+
+    def delta(self, out_removed=None, out_added=None) -> tuple[np.ndarray, np.ndarray]:
+        """(pairs the moved boxes had, pairs they have) of the last move, as
+        host arrays (written into the given arrays -- page-locked ones make
+        the copies fast -- when passed)."""
+        return self._copy(1, self.nremoved, out_removed), self._copy(2, self.nadded, out_added)
+
+    def close(self):
+        if getattr(self, "_sc", None):
+            self._L.pbig2_scene_destroy(self._sc)
+            self._sc = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def tune_shift(boxes: np.ndarray, range_: int, sample: int = 4096) -> int:
