@@ -124,6 +124,20 @@ PBIG2_API int pbig2_batch_intersect(pbig2_ctx* ctx, const uint32_t* boxes,
  * pbig2_set_pair_output when the pairs went there. */
 PBIG2_API int pbig2_result_pairs(pbig2_ctx* ctx, const uint32_t** dev_pairs, uint64_t* npairs);
 
+/* Record mode results (PBIG2_OPT_RICE): device pointers to the stream
+ * (nwords 8-byte words), StartI (ncells values) and Recs (nentries values),
+ * valid until the next query; *npairs of the query counts the pairs in the
+ * records. pbig2_copy_records copies them to host or device buffers (any of
+ * the three may be NULL). pbig2_decode_records decodes a stream held in host
+ * memory into (min, max) pairs. */
+PBIG2_API int pbig2_result_records(pbig2_ctx* ctx, const uint64_t** words, uint64_t* nwords,
+                                   const uint32_t** start_i, uint64_t* ncells, const uint32_t** recs,
+                                   uint64_t* nentries);
+PBIG2_API int pbig2_copy_records(pbig2_ctx* ctx, uint64_t* words, uint32_t* start_i, uint32_t* recs);
+PBIG2_API int pbig2_decode_records(const uint64_t* words, uint64_t nwords, const uint32_t* start_i, uint64_t ncells,
+                                   const uint32_t* recs, uint64_t nentries, uint32_t* pairs, uint64_t cap,
+                                   uint64_t* npairs);
+
 /* Direct pair output (no counterpart in the reference, whose decode() always
  * copies batches out). Later self and bipartite queries on ctx store their
  * pairs straight into dst, cap_pairs pairs of it: device memory, or
@@ -171,6 +185,19 @@ PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
  * block. The pair set is the same; the work statistics (pbig2_stats) are
  * the merged build's. Self and red/blue queries only. */
 #define PBIG2_OPT_MERGED 2
+/* PBIG2_OPT_RICE (default 0): self queries return the reference's Rice
+ * record stream (RICE_COMPRESSION with 8-byte words, writer
+ * src/pbig/pbig.cu:788-920, reader src/pbig/decode.cc:38-131) instead of
+ * flat pairs, for tools that consume that stream: blocks of {0x0fffff11, cell
+ * id} then records {row tile u8, column tile u8, row index u16, hits u16, one
+ * column index u8 per hit} padded to 8 bytes, rows and columns being indices
+ * into the cell's entry list. pbig2_result_records gives the stream and the
+ * two arrays that decode it (StartI: first entry of each cell; Recs: the box
+ * index of each entry); pbig2_decode_records is the reference's decode with
+ * its column-offset bug fixed. Cells of 65536 boxes or more cannot be
+ * written (PBIG2_ECAPACITY). Blocks are per emission step, so one cell can
+ * have several (as the reference's cells of several jobs do). */
+#define PBIG2_OPT_RICE 3
 PBIG2_API int pbig2_set_option(pbig2_ctx* ctx, int option, int64_t value);
 
 /* Allocation-free self-intersection (no counterpart in the reference).

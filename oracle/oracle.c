@@ -545,3 +545,47 @@ void orc_sort_pairs(uint32_t* pairs, uint64_t n) {
     for (uint64_t i = 0; i < n; i++) { pairs[2 * i] = (uint32_t)(k[i] >> 32); pairs[2 * i + 1] = (uint32_t)k[i]; }
     free(k); free(t);
 }
+
+/* ------------------------------------------------------------------ */
+/* decode() of the Rice records, src/pbig/decode.cc:26-138 (RICE_COMPRESSION,
+ * 8-byte words), with the column bytes read where the writer puts them:
+ * record + 6 + k (the reference reads ((i+1)<<3)+2+k = record + 10 + k,
+ * decode.cc:80, against the writer's overcnt = 6, pbig.cu:790, 851). The loop
+ * follows the reference's; it stops at the end of the stream instead of
+ * reading the word after it. Pairs come out as (min, max); returns the pair
+ * count (out may be NULL to count), or -1 on a malformed stream.           */
+/* ------------------------------------------------------------------ */
+int64_t orc_decode_rice(const uint64_t* p, uint64_t cnt, const uint32_t* StartI, uint64_t ncells,
+                        const uint32_t* Recs, uint64_t nrecs, uint32_t* out, uint64_t cap) {
+    const uint64_t UNUSED = 0x0fffff11ull;
+    const unsigned char* bytes = (const unsigned char*)p;
+    const unsigned short* shorts = (const unsigned short*)p;
+    uint64_t np = 0;
+    for (uint64_t i = 2; i < cnt; i += 2) {
+        if (p[i - 2] != UNUSED) return -1;
+        uint64_t gid = p[i - 1];
+        if (gid >= ncells) return -1;
+        do {
+            uint32_t seg1 = bytes[(i << 3) + 0];
+            uint32_t seg2 = bytes[(i << 3) + 1];
+            uint32_t l_rid = shorts[(i << 2) + 1];
+            uint32_t nlaps = shorts[(i << 2) + 2];
+            uint64_t base1 = (uint64_t)StartI[gid] + (seg1 << 8);
+            uint64_t base2 = (uint64_t)StartI[gid] + (seg2 << 8);
+            if (base1 + l_rid >= nrecs) return -1;
+            uint32_t rid1 = Recs[base1 + l_rid];
+            for (uint32_t k = 0; k < nlaps; k++) {
+                uint32_t t = bytes[(i << 3) + 6 + k];
+                if (base2 + t >= nrecs) return -1;
+                uint32_t rid2 = Recs[base2 + t];
+                if (out && np < cap) {
+                    out[2 * np] = rid1 < rid2 ? rid1 : rid2;
+                    out[2 * np + 1] = rid1 < rid2 ? rid2 : rid1;
+                }
+                np++;
+            }
+            i = i + ((6 + nlaps + sizeof(uint64_t) - 1) >> 3);
+        } while (i < cnt && p[i] != UNUSED);
+    }
+    return (int64_t)np;
+}

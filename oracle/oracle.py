@@ -48,6 +48,8 @@ def lib():
         L.orc_gen_harness.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, C.c_char_p, C.c_uint32, C.c_int, u32p]
         L.orc_gen_harness.restype = C.c_int
         L.orc_sort_pairs.argtypes = [u32p, C.c_uint64]
+        L.orc_decode_rice.argtypes = [C.c_void_p, C.c_uint64, u32p, C.c_uint64, u32p, C.c_uint64, u32p, C.c_uint64]
+        L.orc_decode_rice.restype = C.c_int64
         L.orc_sort_pairs.restype = None
         L.orc_srand.argtypes = [C.c_void_p, C.c_uint32]
         L.orc_rand.argtypes = [C.c_void_p]
@@ -125,6 +127,22 @@ def sort_pairs(p: np.ndarray) -> np.ndarray:
     q = np.ascontiguousarray(np.stack([lo, hi], axis=1))
     lib().orc_sort_pairs(_ptr(q), q.shape[0])
     return q
+
+
+def decode_rice(words: np.ndarray, start_i: np.ndarray, recs: np.ndarray) -> np.ndarray:
+    """The reference's decode of a Rice record stream (decode.cc:26-138, with
+    the column offset fixed): [P,2] (min, max) pairs in stream order."""
+    L = lib()
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    si = np.ascontiguousarray(start_i, dtype=np.uint32)
+    rc = np.ascontiguousarray(recs, dtype=np.uint32)
+    args = [w.ctypes.data_as(C.c_void_p), w.shape[0], _ptr(si), si.shape[0], _ptr(rc), rc.shape[0]]
+    n = L.orc_decode_rice(*args, None, 0)
+    if n < 0:
+        raise ValueError("malformed record stream")
+    out = np.empty((n, 2), dtype=np.uint32)
+    L.orc_decode_rice(*args, _ptr(out), n)
+    return out
 
 
 def harness_boxes(n: int, S: int = 100, range_: int = 10000, sim: str = "UU", seed: int = 100,

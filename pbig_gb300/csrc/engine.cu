@@ -308,7 +308,11 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
 // result bookkeeping after a pass: pair count, per-scene offsets, stats
 static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t ncells, uint32_t nsc,
                         const std::vector<GridScene>& scenes, bool grouped, int launches, cudaStream_t st) {
-    c->npairs = h.pairs;
+    c->result_records = c->rice_mode && !grouped;
+    c->rice_words = c->result_records ? h.pairs : 0;
+    c->npairs = c->result_records ? h.rec_pairs : h.pairs;
+    c->last_ncells = ncells;
+    c->last_entries = h.entries;
     c->result = grouped ? c->d_out2.as<uint2>() : c->result_ext ? c->ext_out : c->d_out.as<uint2>();
     if (grouped) {
         CK(c->h_stage.ensure((nsc + 1) * 8));
@@ -317,7 +321,7 @@ static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t nc
         c->scene_pair_off.assign((const uint64_t*)c->h_stage.p, (const uint64_t*)c->h_stage.p + nsc + 1);
     } else {
         c->scene_pair_off.assign(1, 0);
-        c->scene_pair_off.push_back(h.pairs);
+        c->scene_pair_off.push_back(c->npairs);
     }
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
@@ -343,7 +347,7 @@ static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t nc
     s.jobs = h.jobs;
     s.max_cell = h.max_cell ? h.max_cell : (h.entries ? 1u : 0u);
     s.merged_blocks = c->merged_blocks;
-    s.pairs = h.pairs;
+    s.pairs = c->npairs;
     s.cell_shift = scenes.empty() ? 0 : scenes[0].shift;
     s.scenes = nsc;
     s.kernels = (uint32_t)launches;
@@ -598,7 +602,9 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     bool need_full = true;
     // self/bipartite pairs go straight to the caller's buffer when one is set;
     // a result that does not fit is redone into the context's buffer
-    bool use_ext = c->ext_out != nullptr && !grouped;
+    p.records = (c->rice_mode && !grouped) ? 1u : 0u;
+    if (p.records && split != kNoSplit) return fail(PBIG2_EINVAL, "record mode serves self queries only");
+    bool use_ext = c->ext_out != nullptr && !grouped && !p.records;
     c->result_ext = false;
     for (int attempt = 0; attempt < 6; attempt++) {
         int rc = ensure_query_buffers(c, p, entry_cap, use_ext ? 1 : out_cap, task_cap, nsc, grouped, st);
@@ -614,7 +620,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
                 return fail(PBIG2_ECUDA, "pipeline launch (engine.cu:%d): %s", g_record_line, cudaGetErrorString(re));
         }
         launches += need_full ? 6 : 0;  // count, scan (3), expand, scatter
-        launches += 3 + (grouped ? 3 : 0);
+        launches += 3 + (grouped ? 3 : 0) + (p.records ? 1 : 0);
         CK(cudaMemcpyAsync(c->h_ctr.p, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, st));
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
@@ -624,6 +630,8 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         if (h.err & kErrWait) {
             return fail(PBIG2_ETIMEOUT, "a bounded device wait gave up (scan bulk copy)");
         }
+        if (h.err & kErrRecCell)
+            return fail(PBIG2_ECAPACITY, "a cell of 65536 boxes or more cannot be written as records");
         if (h.err & kErrIndex) {
             return fail(PBIG2_ECUDA, "inconsistent cell lists (error bits 0x%x)", h.err);
         }
@@ -921,6 +929,7 @@ PBIG2_API int pbig2_result_pairs(pbig2_ctx* c, const uint32_t** dev_pairs, uint6
 PBIG2_API int pbig2_copy_pairs(pbig2_ctx* c, uint32_t* dst, uint64_t first, uint64_t count, int dst_loc,
                                void* stream) {
     if (!c || (count && !dst)) return fail(PBIG2_EINVAL, "bad arguments");
+    if (c->result_records) return fail(PBIG2_EINVAL, "the last result is a record stream (pbig2_result_records)");
     if (first > c->npairs || count > c->npairs - first) return fail(PBIG2_EINVAL, "range beyond the result");
     if (count == 0) return PBIG2_OK;
     CK(cudaSetDevice(c->device));
@@ -935,6 +944,7 @@ PBIG2_API int pbig2_copy_pairs(pbig2_ctx* c, uint32_t* dst, uint64_t first, uint
 PBIG2_API int pbig2_copy_pairs_async(pbig2_ctx* c, uint32_t* dst, uint64_t first, uint64_t count, int dst_loc,
                                      void* stream) {
     if (!c || (count && !dst)) return fail(PBIG2_EINVAL, "bad arguments");
+    if (c->result_records) return fail(PBIG2_EINVAL, "the last result is a record stream (pbig2_result_records)");
     if (first > c->npairs || count > c->npairs - first) return fail(PBIG2_EINVAL, "range beyond the result");
     if (count == 0) return PBIG2_OK;
     CK(cudaSetDevice(c->device));
@@ -942,6 +952,72 @@ PBIG2_API int pbig2_copy_pairs_async(pbig2_ctx* c, uint32_t* dst, uint64_t first
     if ((const void*)dst == (const void*)(c->result + first)) return PBIG2_OK;  // already there
     CK(cudaMemcpyAsync(dst, c->result + first, count * 8, cudaMemcpyDefault, pick_stream(c, stream)));
     return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_result_records(pbig2_ctx* c, const uint64_t** words, uint64_t* nwords, const uint32_t** start_i,
+                                   uint64_t* ncells, const uint32_t** recs, uint64_t* nentries) {
+    if (!c || !words || !nwords || !start_i || !ncells || !recs || !nentries) return fail(PBIG2_EINVAL, "bad arguments");
+    if (!c->result_records) return fail(PBIG2_EINVAL, "the last result is not a record stream (PBIG2_OPT_RICE)");
+    *words = reinterpret_cast<const uint64_t*>(c->result);
+    *nwords = c->rice_words;
+    *start_i = c->d_counts.as<uint32_t>();
+    *ncells = c->last_ncells;
+    *recs = c->d_entries.as<uint32_t>();
+    *nentries = c->last_entries;
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_copy_records(pbig2_ctx* c, uint64_t* words, uint32_t* start_i, uint32_t* recs) {
+    if (!c || (!words && !start_i && !recs)) return fail(PBIG2_EINVAL, "bad arguments");
+    if (!c->result_records) return fail(PBIG2_EINVAL, "the last result is not a record stream (PBIG2_OPT_RICE)");
+    CK(cudaSetDevice(c->device));
+    cudaStream_t st = c->own_stream;
+    if (words && c->rice_words) CK(cudaMemcpyAsync(words, c->result, c->rice_words * 8, cudaMemcpyDefault, st));
+    if (start_i && c->last_ncells) CK(cudaMemcpyAsync(start_i, c->d_counts.p, c->last_ncells * 4, cudaMemcpyDefault, st));
+    if (recs && c->last_entries) CK(cudaMemcpyAsync(recs, c->d_entries.p, c->last_entries * 4, cudaMemcpyDefault, st));
+    CK(cudaStreamSynchronize(st));
+    return PBIG2_OK;
+}
+
+// the reference's decode() (src/pbig/decode.cc:26-138) for the Rice records,
+// with the column bytes read where the writer puts them (record + 6 + k;
+// the reference reads record + 10 + k, decode.cc:80 against pbig.cu:851)
+PBIG2_API int pbig2_decode_records(const uint64_t* w, uint64_t nwords, const uint32_t* start_i, uint64_t ncells,
+                                   const uint32_t* recs, uint64_t nentries, uint32_t* pairs, uint64_t cap,
+                                   uint64_t* npairs) {
+    if (!npairs || (nwords && (!w || !start_i || !recs)) || (cap && !pairs)) return fail(PBIG2_EINVAL, "bad arguments");
+    const uint64_t kUnused = 0x0fffff11ull;
+    uint64_t np = 0, i = 0;
+    while (i < nwords) {
+        if (w[i] != kUnused || i + 1 >= nwords) return fail(PBIG2_EINPUT, "record stream: block header expected at word %llu", (unsigned long long)i);
+        const uint64_t gid = w[i + 1];
+        if (gid >= ncells) return fail(PBIG2_EINPUT, "record stream: cell %llu out of range", (unsigned long long)gid);
+        i += 2;
+        while (i < nwords && w[i] != kUnused) {
+            const unsigned char* r = reinterpret_cast<const unsigned char*>(w + i);
+            const uint32_t seg1 = r[0], seg2 = r[1];
+            const uint32_t lrow = (uint32_t)r[2] | ((uint32_t)r[3] << 8);
+            const uint32_t nh = (uint32_t)r[4] | ((uint32_t)r[5] << 8);
+            const uint64_t len = (6u + nh + 7u) >> 3;
+            if (i + len > nwords) return fail(PBIG2_EINPUT, "record stream: record past the end");
+            const uint64_t base1 = (uint64_t)start_i[gid] + (seg1 << 8), base2 = (uint64_t)start_i[gid] + (seg2 << 8);
+            if (base1 + lrow >= nentries) return fail(PBIG2_EINPUT, "record stream: row past the entries");
+            const uint32_t a = recs[base1 + lrow];
+            for (uint32_t k = 0; k < nh; k++) {
+                const uint64_t e = base2 + r[6 + k];
+                if (e >= nentries) return fail(PBIG2_EINPUT, "record stream: column past the entries");
+                const uint32_t b = recs[e];
+                if (np < cap) {
+                    pairs[2 * np] = a < b ? a : b;
+                    pairs[2 * np + 1] = a < b ? b : a;
+                }
+                np++;
+            }
+            i += len;
+        }
+    }
+    *npairs = np;
+    return np <= cap ? PBIG2_OK : fail(PBIG2_ECAPACITY, "pair buffer too small; *npairs holds the pair count");
 }
 
 PBIG2_API int pbig2_set_pair_output(pbig2_ctx* c, uint32_t* dst, uint64_t cap_pairs) {
@@ -1000,6 +1076,10 @@ PBIG2_API int pbig2_set_option(pbig2_ctx* c, int option, int64_t value) {
     }
     if (option == PBIG2_OPT_MERGED) {
         c->merged_mode = value != 0;
+        return PBIG2_OK;
+    }
+    if (option == PBIG2_OPT_RICE) {
+        c->rice_mode = value != 0;
         return PBIG2_OK;
     }
     return fail(PBIG2_EINVAL, "unknown option %d", option);

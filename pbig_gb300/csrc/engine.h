@@ -55,6 +55,10 @@ struct pbig2_ctx {
     cudaEvent_t evp[9] = {};
     pbig::DevBuf d_merged;  // merged mode: cell -> root table
     bool merged_mode = false;
+    bool rice_mode = false;      // record mode (PBIG2_OPT_RICE)
+    bool result_records = false; // the last result is a record stream
+    uint64_t rice_words = 0;     // words of the last record stream
+    uint64_t last_ncells = 0, last_entries = 0;
     uint32_t merged_blocks = 0;  // merged blocks of the last query
     pbig::DevBuf d_boxes, d_counts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
         d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims;

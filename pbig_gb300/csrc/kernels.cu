@@ -583,7 +583,8 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_scan_cells(Params pin) {
                         rk = pk6_excl++;
                     }
                     const uint64_t idx = (uint64_t)b + rk;
-                    if (idx < pin.list_cap[c]) p.lists[pin.list_off[c] + idx] = make_uint2(st[k], v[k]);
+                    const uint32_t key = p.records ? (uint32_t)(chunk_cell(ch, k >> 2) + (k & 3)) : st[k];
+                    if (idx < pin.list_cap[c]) p.lists[pin.list_off[c] + idx] = make_uint2(key, v[k]);
                 }
             }
         }
@@ -756,6 +757,7 @@ struct WarpOut {
     uint2* buf;
     uint32_t n;    // warp-uniform fill
     uint32_t cap;  // buffer capacity (pairs)
+    unsigned long long hits = 0;  // record mode: pairs written by this lane
 };
 
 __device__ __forceinline__ void wflush(const Params& p, WarpOut& o) {
@@ -822,9 +824,86 @@ __device__ __forceinline__ void wemit(const Params& p, WarpOut& o, uint32_t ma, 
     if (!direct) o.n += total;
 }
 
+// ---- record mode: the reference's Rice stream ------------------------------
+// (RICE_COMPRESSION with 8-byte OTYPE: writer src/pbig/pbig.cu:788-920, reader
+// src/pbig/decode.cc:38-131). A block is the header {UNUSED, cell id} followed
+// by records; a record is one row box's hits in one 256-column tile of the
+// cell: byte 0 row tile (row >> 8), byte 1 column tile, bytes 2-3 the row's
+// index in its tile, bytes 4-5 the hit count, then one byte per hit (the
+// column's index in its tile), padded to 8 bytes. Rows and columns are
+// indices into the cell's entry list. Here a block is written per emission
+// step (a cell may have several blocks, as the reference's cells of several
+// jobs do), and a record covers one 32-column tile or the diagonal sweep.
+constexpr unsigned long long kRiceUnused = 0x0fffff11ull;  // UNUSED, the block marker
+
+__device__ __forceinline__ uint32_t rec_words(uint32_t hits) { return hits ? (6u + hits + 7u) >> 3 : 0u; }
+
+// one record: `row` and the columns loc(bit) of the set bits of m (all in one
+// 256-column tile) into dst, or nowhere when `keep` is false
+template <class L>
+__device__ __forceinline__ void rec_write(unsigned long long* dst, bool keep, uint32_t row, uint32_t m, L loc) {
+    const uint32_t nh = __popc(m);
+    unsigned long long word = (unsigned long long)(row >> 8) | ((unsigned long long)(loc(__ffs(m) - 1) >> 8) << 8) |
+                              ((unsigned long long)(row & 255u) << 16) | ((unsigned long long)nh << 32);
+    uint32_t byte = 6, wi = 0;
+    while (m) {
+        const uint32_t b = __ffs(m) - 1;
+        m &= m - 1;
+        word |= (unsigned long long)(loc(b) & 255u) << (8 * byte);
+        if (++byte == 8) {
+            if (keep) dst[wi] = word;
+            wi++;
+            word = 0;
+            byte = 0;
+        }
+    }
+    if (byte && keep) dst[wi] = word;
+}
+
+// warp step: lane records for ma (columns la) and mb (columns lb), one block
+// header per cell before its first record; gmask: the lanes of this lane's
+// cell (the whole warp, or a lane group of the small-cell kernel)
+template <class LA, class LB>
+__device__ __forceinline__ void remit(const Params& p, WarpOut& o, uint32_t ma, LA la, uint32_t mb, LB lb,
+                                      uint32_t row, uint32_t gid, uint32_t gmask) {
+    const uint32_t lane = lane_id();
+    const uint32_t wa = rec_words(__popc(ma)), wb = rec_words(__popc(mb));
+    const uint32_t gany = __ballot_sync(FULL_MASK, (wa | wb) != 0u) & gmask;
+    const bool hdr = gany != 0u && lane == (uint32_t)(__ffs(gany) - 1);
+    const uint32_t k = wa + wb + (hdr ? 2u : 0u);
+    const uint32_t incl = warp_incl_scan(k);
+    const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+    if (total == 0) return;
+    o.hits += __popc(ma) + __popc(mb);
+    bool direct = false;
+    unsigned long long gbase = 0;
+    if (o.n + total > o.cap) {
+        wflush(p, o);
+        if (total > o.cap) {
+            direct = true;
+            if (lane == 0) gbase = atomicAdd(&p.ctr->pairs, (unsigned long long)total);
+            gbase = __shfl_sync(FULL_MASK, gbase, 0);
+        }
+    }
+    const bool keep = !direct || gbase + total <= p.out_cap;
+    if (direct && !keep && lane == 0) atomicOr(&p.ctr->err, kErrOutOvf);
+    unsigned long long* dst = direct ? reinterpret_cast<unsigned long long*>(p.out) + gbase
+                                     : reinterpret_cast<unsigned long long*>(o.buf + o.n);
+    uint32_t w = incl - k;
+    if (hdr && keep) {
+        dst[w] = kRiceUnused;
+        dst[w + 1] = gid;
+    }
+    if (hdr) w += 2;
+    if (wa) rec_write(dst + w, keep, row, ma, la);
+    if (wb) rec_write(dst + w + wa, keep, row, mb, lb);
+    __syncwarp();
+    if (!direct) o.n += total;
+}
+
 // row tile r of a cell staged at slots [off, off + n8): the diagonal tile and
 // every column tile x > r, emitted two tiles at a time
-template <int D, bool BIP, bool NARROW, class Emit>
+template <int D, bool BIP, bool NARROW, bool REC, class Emit>
 __device__ __forceinline__ void row_unit(const Params& p, const Slots& s, uint32_t off, uint32_t n, uint32_t r,
                                          Emit emit) {
     const uint32_t lane = lane_id();
@@ -833,6 +912,34 @@ __device__ __forceinline__ void row_unit(const Params& p, const Slots& s, uint32
     const uint32_t rbase = off + 32 * r;
     const Box me = lane < rows ? slot_get(s, rbase + lane) : dummy_box<NARROW>();
     const uint32_t md = sweep_diag<D, BIP, NARROW>(s, me, lane, rbase, rows, p.split);
+    if constexpr (REC) {  // records: cell-local row and column indices
+        const uint32_t row = 32 * r + lane;
+        auto ldiag = [&](uint32_t d) {
+            uint32_t pr = lane + d;
+            if (pr >= rows) pr -= rows;
+            return 32 * r + pr;
+        };
+        uint32_t x = r + 1;
+        if (x >= R) {
+            emit(md, ldiag, 0u, ldiag, row);
+            return;
+        }
+        {
+            const uint32_t cb = off + 32 * x, c8 = (min(32u, n - 32 * x) + 7) & ~7u;
+            const uint32_t mc = sweep_cols<D, BIP, NARROW>(s, me, cb, c8, p.split);
+            emit(md, ldiag, mc, [&](uint32_t j) { return 32 * x + j; }, row);
+        }
+        for (x = r + 2; x < R; x += 2) {
+            const uint32_t cb1 = off + 32 * x, c81 = (min(32u, n - 32 * x) + 7) & ~7u;
+            const uint32_t m1 = sweep_cols<D, BIP, NARROW>(s, me, cb1, c81, p.split);
+            uint32_t m2 = 0;
+            if (x + 1 < R)
+                m2 = sweep_cols<D, BIP, NARROW>(s, me, off + 32 * (x + 1), (min(32u, n - 32 * (x + 1)) + 7) & ~7u,
+                                                p.split);
+            emit(m1, [&](uint32_t j) { return 32 * x + j; }, m2, [&](uint32_t j) { return 32 * (x + 1) + j; }, row);
+        }
+        return;
+    }
     auto pdiag = [&](uint32_t d) {
         uint32_t pr = lane + d;
         if (pr >= rows) pr -= rows;
@@ -864,23 +971,28 @@ __device__ __forceinline__ void row_unit(const Params& p, const Slots& s, uint32
 // ---- small cells ------------------------------------------------------------
 // lane group g (WG lanes) holds cell item*G+g of the class list, lane r its
 // box r; the circular half sweep runs inside the group.
-template <int D, int WG, bool NARROW>
+template <int D, int WG, bool NARROW, bool REC>
 __device__ __forceinline__ Box small_fetch(const Params& p, int list, uint64_t nl, uint64_t ci, uint32_t r,
-                                           uint32_t& n) {
+                                           uint32_t& n, uint32_t& gid) {
     n = 0;
+    gid = 0;
     uint32_t start = 0;
     if (ci < nl) {
         const uint2 sn = p.lists[p.list_off[list] + ci];
         start = sn.x;
         n = sn.y;
+        if (REC) {  // the list holds the cell id; its start is in the counters after the scatter
+            gid = sn.x;
+            start = gid < p.ncells ? p.counts[gid] : 0xffffffffu;
+        }
         if (n > WG || (uint64_t)start + n > p.entry_cap) n = 0;  // inconsistent grid: skip
     }
     return r < n ? load_box<D, NARROW>(p, p.entries[start + r]) : dummy_box<NARROW>();
 }
 
-template <int D, int WG, bool BIP, bool NARROW>
+template <int D, int WG, bool BIP, bool NARROW, bool REC>
 __device__ __forceinline__ void small_sweep(const Params& p, const Slots& s, WarpOut& o, const Box& me, uint32_t n,
-                                            uint32_t lane, uint32_t g, uint32_t r) {
+                                            uint32_t lane, uint32_t g, uint32_t r, uint32_t gid) {
     slot_put(s, lane, me);
     __syncwarp();
     const uint32_t gb = g * WG;
@@ -893,15 +1005,25 @@ __device__ __forceinline__ void small_sweep(const Params& p, const Slots& s, War
         if (pr >= WG) pr = 0;  // idle lanes (n = 0) stay inside the group
         mask |= (hit_bit<D, BIP, NARROW>(me, slot_get(s, gb + pr), p.split) & (d <= nelm ? 1u : 0u)) << d;
     }
-    auto pid = [&](uint32_t d) {
-        uint32_t pr = r + d;
-        if (pr >= n) pr -= n;
-        return slot_id(s, gb + pr);
-    };
-    wemit<BIP>(p, o, mask, pid, 0u, pid, me.id);
+    if constexpr (REC) {
+        auto ploc = [&](uint32_t d) {
+            uint32_t pr = r + d;
+            if (pr >= n) pr -= n;
+            return pr;
+        };
+        const uint32_t gmask = WG == 32 ? FULL_MASK : (((1u << WG) - 1u) << (g * WG));
+        remit(p, o, mask, ploc, 0u, ploc, r, gid, gmask);
+    } else {
+        auto pid = [&](uint32_t d) {
+            uint32_t pr = r + d;
+            if (pr >= n) pr -= n;
+            return slot_id(s, gb + pr);
+        };
+        wemit<BIP>(p, o, mask, pid, 0u, pid, me.id);
+    }
 }
 
-template <int D, int WG, bool BIP, bool NARROW>
+template <int D, int WG, bool BIP, bool NARROW, bool REC>
 __device__ __forceinline__ void small_items(const Params& p, const Slots& s, WarpOut& o, int list, uint64_t first,
                                             uint64_t stride) {
     constexpr uint32_t G = 32 / WG;
@@ -909,13 +1031,19 @@ __device__ __forceinline__ void small_items(const Params& p, const Slots& s, War
     const uint64_t nl = mn64(p.ctr->n_list[list], p.list_cap[list]);
     const uint64_t nitems = (nl + G - 1) / G;
     for (uint64_t item = first; item < nitems; item += stride) {
-        uint32_t n1;
-        const Box a = small_fetch<D, WG, NARROW>(p, list, nl, item * G + g, r, n1);
-        small_sweep<D, WG, BIP, NARROW>(p, s, o, a, n1, lane, g, r);
+        uint32_t n1, gid;
+        const Box a = small_fetch<D, WG, NARROW, REC>(p, list, nl, item * G + g, r, n1, gid);
+        small_sweep<D, WG, BIP, NARROW, REC>(p, s, o, a, n1, lane, g, r, gid);
     }
 }
 
-template <int D, bool BIP, bool NARROW>
+// hits of a warp's records, added to the query's pair count
+__device__ __forceinline__ void rec_hits(const Params& p, const WarpOut& o) {
+    const unsigned long long h = warp_sum_u64(o.hits);
+    if (lane_id() == 0 && h) atomicAdd(&p.ctr->rec_pairs, h);
+}
+
+template <int D, bool BIP, bool NARROW, bool REC = false>
 __global__ void __launch_bounds__(kPairThreads, 6) k_pairs_small(Params p) {
     __shared__ uint4 s_a[kPairWarps][kSmallSlots], s_b[kPairWarps][kSmallSlots];
     __shared__ uint2 s_out[kPairWarps][kWarpOut];
@@ -924,11 +1052,12 @@ __global__ void __launch_bounds__(kPairThreads, 6) k_pairs_small(Params p) {
     WarpOut o{s_out[warp], 0, kWarpOut};
     const uint64_t gw = (uint64_t)blockIdx.x * kPairWarps + warp, nw = (uint64_t)gridDim.x * kPairWarps;
     // classes interleaved over the warps so every warp gets a similar mix
-    small_items<D, 32, BIP, NARROW>(p, s, o, 3, gw, nw);
-    small_items<D, 16, BIP, NARROW>(p, s, o, 2, (gw + nw / 4) % nw, nw);
-    small_items<D, 8, BIP, NARROW>(p, s, o, 1, (gw + nw / 2) % nw, nw);
-    small_items<D, 4, BIP, NARROW>(p, s, o, 0, (gw + 3 * nw / 4) % nw, nw);
+    small_items<D, 32, BIP, NARROW, REC>(p, s, o, 3, gw, nw);
+    small_items<D, 16, BIP, NARROW, REC>(p, s, o, 2, (gw + nw / 4) % nw, nw);
+    small_items<D, 8, BIP, NARROW, REC>(p, s, o, 1, (gw + nw / 2) % nw, nw);
+    small_items<D, 4, BIP, NARROW, REC>(p, s, o, 0, (gw + 3 * nw / 4) % nw, nw);
     wflush(p, o);
+    if (REC) rec_hits(p, o);
 }
 
 // ---- medium cells: one per warp item, staged whole ---------------------------
@@ -1034,7 +1163,7 @@ __device__ __forceinline__ uint32_t diag_allow(uint32_t allow, uint32_t lane, ui
     return a;
 }
 
-template <int D, bool BIP, bool NARROW>
+template <int D, bool BIP, bool NARROW, bool REC = false>
 __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -1046,7 +1175,8 @@ __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
     const uint64_t nw = (uint64_t)gridDim.x * kPairWarps;
     for (uint64_t item = (uint64_t)blockIdx.x * kPairWarps + warp; item < nl; item += nw) {
         const uint2 sn = p.lists[p.list_off[kListMed] + item];
-        const uint32_t start = sn.x;
+        const uint32_t gid = sn.x;  // record mode: the cell id (its start is in the counters)
+        const uint32_t start = REC ? (gid < p.ncells ? p.counts[gid] : 0xffffffffu) : sn.x;
         const uint32_t n = sn.y;
         if (n > kMedMax || (uint64_t)start + n > p.entry_cap) continue;  // inconsistent grid: skip
         const uint32_t R = (n + 31) >> 5;
@@ -1086,18 +1216,40 @@ __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
                 if (__any_sync(FULL_MASK, allow != 0u))
                     mc = sweep_tile<D, NARROW>(s, me, c0, cnt) & (__brev(allow) >> (32u - cnt));
                 auto pcol = [&](uint32_t k) { return slot_id(s, c0 + cnt - 1 - k); };
-                if (have) {
+                if constexpr (REC) {
+                    auto lcol = [&](uint32_t k) { return c0 + cnt - 1 - k; };
+                    auto ldiag = [&](uint32_t k) {
+                        uint32_t pr = l + dmax - k;
+                        if (pr >= rows) pr -= rows;
+                        return rb + pr;
+                    };
+                    if (have) remit(p, o, pend, ldiag, mc, lcol, rb + lane, gid, FULL_MASK);
+                    else remit(p, o, mc, lcol, 0u, lcol, rb + lane, gid, FULL_MASK);
+                    have = false;
+                } else if (have) {
                     wemit<BIP>(p, o, pend, pdiag, mc, pcol, me.id);
                     have = false;
                 } else {
                     wemit<BIP>(p, o, mc, pcol, 0u, pcol, me.id);
                 }
             }
-            if (have) wemit<BIP>(p, o, pend, pdiag, 0u, pdiag, me.id);
+            if (have) {
+                if constexpr (REC) {
+                    auto ldiag = [&](uint32_t k) {
+                        uint32_t pr = l + dmax - k;
+                        if (pr >= rows) pr -= rows;
+                        return rb + pr;
+                    };
+                    remit(p, o, pend, ldiag, 0u, ldiag, rb + lane, gid, FULL_MASK);
+                } else {
+                    wemit<BIP>(p, o, pend, pdiag, 0u, pdiag, me.id);
+                }
+            }
         }
         __syncwarp();
     }
     wflush(p, o);
+    if (REC) rec_hits(p, o);
 }
 
 // ---- big cells (block staged) and huge cells (tiles) -----------------------
@@ -1111,6 +1263,8 @@ struct BlockSmem {
     uint32_t unit_pref[kBigCellsPerTask + 1];
     uint32_t k, tot, units;
     unsigned long long nbt[2];
+    uint32_t cell_gid[kBigCellsPerTask];  // record mode: cell ids
+    unsigned long long hits;              // record mode: pairs written by the block
 };
 
 // block-buffer compaction (shared reservation per warp call); when the
@@ -1160,7 +1314,48 @@ __device__ __forceinline__ void bemit(const Params& p, BlockSmem& s, uint32_t ma
     }
 }
 
-template <int D, bool BIP, bool NARROW>
+// block-buffer record step (the words of a warp step go to the block buffer
+// or, when it is full, straight to global memory)
+template <class LA, class LB>
+__device__ __forceinline__ void bremit(const Params& p, BlockSmem& s, uint32_t ma, LA la, uint32_t mb, LB lb,
+                                       uint32_t row, uint32_t gid) {
+    const uint32_t lane = lane_id();
+    const uint32_t wa = rec_words(__popc(ma)), wb = rec_words(__popc(mb));
+    const uint32_t any = __ballot_sync(FULL_MASK, (wa | wb) != 0u);
+    const bool hdr = any != 0u && lane == (uint32_t)(__ffs(any) - 1);
+    const uint32_t k = wa + wb + (hdr ? 2u : 0u);
+    const uint32_t incl = warp_incl_scan(k);
+    const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
+    if (total == 0) return;
+    const unsigned long long hits = warp_sum_u64(__popc(ma) + __popc(mb));
+    uint32_t pos = 0;
+    unsigned long long gbase = 0;
+    if (lane == 0) {
+        atomicAdd(&s.hits, hits);
+        pos = atomicAdd(&s.out_n, total);
+        if (pos + total > kBlockOut) {
+            atomicMin(&s.first_ovf, pos);
+            gbase = atomicAdd(&p.ctr->pairs, (unsigned long long)total);
+        }
+    }
+    pos = __shfl_sync(FULL_MASK, pos, 0);
+    gbase = __shfl_sync(FULL_MASK, gbase, 0);
+    const bool direct = pos + total > kBlockOut;
+    const bool keep = !direct || gbase + total <= p.out_cap;
+    if (direct && !keep && lane == 0) atomicOr(&p.ctr->err, kErrOutOvf);
+    unsigned long long* dst = direct ? reinterpret_cast<unsigned long long*>(p.out) + gbase
+                                     : reinterpret_cast<unsigned long long*>(s.out + pos);
+    uint32_t w = incl - k;
+    if (hdr && keep) {
+        dst[w] = kRiceUnused;
+        dst[w + 1] = gid;
+    }
+    if (hdr) w += 2;
+    if (wa) rec_write(dst + w, keep, row, ma, la);
+    if (wb) rec_write(dst + w + wa, keep, row, mb, lb);
+}
+
+template <int D, bool BIP, bool NARROW, bool REC>
 __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const Slots sl{s.a, s.b};
@@ -1172,10 +1367,15 @@ __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
         if (warp == 0) {
             uint32_t n = 0, st = 0;
             const bool v = lane < kBigCellsPerTask && cur + lane < end;
+            uint32_t gid = 0;
             if (v) {
                 const uint2 sn = p.lists[p.list_off[kListBig] + cur + lane];
                 st = sn.x;
                 n = sn.y;
+                if (REC) {  // the list holds the cell id; its start is in the counters
+                    gid = sn.x;
+                    st = gid < p.ncells ? p.counts[gid] : 0xffffffffu;
+                }
                 if (n > kBigMax || (uint64_t)st + n > p.entry_cap) n = 0;  // inconsistent grid: skip
             }
             const uint32_t n8 = (n + 7) & ~7u;
@@ -1186,6 +1386,7 @@ __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
             const uint32_t uinc = warp_incl_scan(units);
             if (lane < k) {
                 s.cell_start[lane] = st;
+                s.cell_gid[lane] = gid;
                 s.cell_n[lane] = n;
                 s.cell_off[lane] = inc - n8;
                 s.unit_pref[lane + 1] = uinc;
@@ -1219,7 +1420,15 @@ __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
 #pragma unroll
             for (uint32_t step = 4; step; step >>= 1)
                 if (c + step < K && s.unit_pref[c + step] <= u) c += step;
-            row_unit<D, BIP, NARROW>(p, sl, s.cell_off[c], s.cell_n[c], u - s.unit_pref[c], emit);
+            if constexpr (REC) {
+                const uint32_t gid = s.cell_gid[c];
+                auto remit_b = [&](uint32_t ma, auto la, uint32_t mb, auto lb, uint32_t row) {
+                    bremit(p, s, ma, la, mb, lb, row, gid);
+                };
+                row_unit<D, BIP, NARROW, true>(p, sl, s.cell_off[c], s.cell_n[c], u - s.unit_pref[c], remit_b);
+            } else {
+                row_unit<D, BIP, NARROW, false>(p, sl, s.cell_off[c], s.cell_n[c], u - s.unit_pref[c], emit);
+            }
         }
         __syncthreads();
         cur += K;
@@ -1228,14 +1437,20 @@ __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
 
 // huge cells: one tile task {start, n, r, x0} per warp; boxes gathered per
 // tile into the warp's 64 slots (32 rows, 32 columns)
-template <int D, bool BIP, bool NARROW>
+template <int D, bool BIP, bool NARROW, bool REC>
 __device__ __forceinline__ void huge_item(const Params& p, BlockSmem& s, uint64_t item, uint32_t slot0) {
     const uint32_t lane = lane_id();
     const Slots sl{s.a, s.b};
     const uint64_t nt = mn64(p.ctr->need_tasks, p.task_cap);
     if (item >= nt) return;
     const uint4 tk = p.tasks[item];
-    const uint32_t start = tk.x, n = tk.y, r = tk.z, x0 = tk.w;
+    const uint32_t gid = tk.x;  // record mode: the cell id; its start is in the counters
+    const uint32_t start = REC ? (gid < p.ncells ? p.counts[gid] : 0xffffffffu) : tk.x;
+    const uint32_t n = tk.y, r = tk.z, x0 = tk.w;
+    if (REC && n >= 65536u) {  // beyond the record format (u8 row tile)
+        if (lane == 0) atomicOr(&p.ctr->err, kErrRecCell);
+        return;
+    }
     const uint32_t R = (n + 31) >> 5;
     const uint32_t x1 = min(x0 + kTaskCols, R);
     if ((uint64_t)start + n > p.entry_cap || r >= R || x0 >= R) return;
@@ -1246,26 +1461,40 @@ __device__ __forceinline__ void huge_item(const Params& p, BlockSmem& s, uint64_
     for (uint32_t x = x0; x < x1; x++) {
         if (x == r) {
             const uint32_t md = sweep_diag<D, BIP, NARROW>(sl, me, lane, slot0, rows, p.split);
-            auto pd = [&](uint32_t d) {
-                uint32_t pr = lane + d;
-                if (pr >= rows) pr -= rows;
-                return slot_id(sl, slot0 + pr);
-            };
-            bemit<BIP>(p, s, md, pd, 0u, pd, me.id);
+            if constexpr (REC) {
+                auto ld = [&](uint32_t d) {
+                    uint32_t pr = lane + d;
+                    if (pr >= rows) pr -= rows;
+                    return 32 * r + pr;
+                };
+                bremit(p, s, md, ld, 0u, ld, 32 * r + lane, gid);
+            } else {
+                auto pd = [&](uint32_t d) {
+                    uint32_t pr = lane + d;
+                    if (pr >= rows) pr -= rows;
+                    return slot_id(sl, slot0 + pr);
+                };
+                bemit<BIP>(p, s, md, pd, 0u, pd, me.id);
+            }
         } else {
             const uint32_t cols = min(32u, n - 32 * x);
             slot_put(sl, slot0 + 32 + lane,
                      lane < cols ? load_box<D, NARROW>(p, p.entries[start + 32 * x + lane]) : dummy_box<NARROW>());
             __syncwarp();
             const uint32_t mc = sweep_cols<D, BIP, NARROW>(sl, me, slot0 + 32, (cols + 7) & ~7u, p.split);
-            auto pc = [&](uint32_t j) { return slot_id(sl, slot0 + 32 + j); };
-            bemit<BIP>(p, s, mc, pc, 0u, pc, me.id);
+            if constexpr (REC) {
+                auto lc = [&](uint32_t j) { return 32 * x + j; };
+                bremit(p, s, mc, lc, 0u, lc, 32 * r + lane, gid);
+            } else {
+                auto pc = [&](uint32_t j) { return slot_id(sl, slot0 + 32 + j); };
+                bemit<BIP>(p, s, mc, pc, 0u, pc, me.id);
+            }
         }
         __syncwarp();
     }
 }
 
-template <int D, bool BIP, bool NARROW>
+template <int D, bool BIP, bool NARROW, bool REC = false>
 __global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BlockSmem& s = *reinterpret_cast<BlockSmem*>(smem_raw);
@@ -1273,6 +1502,7 @@ __global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
     if (t == 0) {
         s.out_n = 0;
         s.first_ovf = kBlockOut;
+        s.hits = 0;
         const uint64_t nb = mn64(p.ctr->n_list[kListBig], p.list_cap[kListBig]);
         const uint64_t nt = mn64(p.ctr->need_tasks, p.task_cap);
         s.nbt[0] = (nb + kBigCellsPerTask - 1) / kBigCellsPerTask;
@@ -1281,8 +1511,8 @@ __global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
     __syncthreads();
     const uint64_t total = s.nbt[0] + s.nbt[1];
     for (uint64_t bt = blockIdx.x; bt < total; bt += gridDim.x) {
-        if (bt < s.nbt[0]) big_task<D, BIP, NARROW>(p, s, bt);
-        else huge_item<D, BIP, NARROW>(p, s, (bt - s.nbt[0]) * kPairWarps + warp, warp * 64);
+        if (bt < s.nbt[0]) big_task<D, BIP, NARROW, REC>(p, s, bt);
+        else huge_item<D, BIP, NARROW, REC>(p, s, (bt - s.nbt[0]) * kPairWarps + warp, warp * 64);
         __syncthreads();
         const uint32_t on = s.out_n, ovf = s.first_ovf;
         const uint32_t nv = min(on, ovf);
@@ -1304,6 +1534,16 @@ __global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
             __syncthreads();
         }
     }
+    if (REC && t == 0 && s.hits) atomicAdd(&p.ctr->rec_pairs, s.hits);
+}
+
+// record mode, after the pair kernels: entries become the plain box indices
+// the record decoder reads (the reference's Recs array)
+__global__ void k_strip_entries(Params pin) {
+    const Params p = resolve(pin);
+    const uint64_t n = mn64(p.ctr->entries, p.entry_cap);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        p.entries[i] &= kIdMask;
 }
 
 // ---------------------------------------------------------------------------
@@ -1405,11 +1645,11 @@ static size_t med_smem() { return (size_t)kPairWarps * (2 * kMedSlots * sizeof(u
 
 size_t pair_smem_bytes() { return sizeof(BlockSmem); }
 
-template <int D, bool B, bool N>
+template <int D, bool B, bool N, bool R = false>
 static cudaError_t init_variant() {
-    cudaError_t e = cudaFuncSetAttribute(k_pairs_med<D, B, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)med_smem());
+    cudaError_t e = cudaFuncSetAttribute(k_pairs_med<D, B, N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)med_smem());
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_pairs_block<D, B, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BlockSmem));
+    e = cudaFuncSetAttribute(k_pairs_block<D, B, N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BlockSmem));
     return e;
 }
 
@@ -1428,6 +1668,10 @@ cudaError_t kernels_init() {
     if ((e = init_variant<3, false, false>()) != cudaSuccess) return e;
     if ((e = init_variant<2, true, false>()) != cudaSuccess) return e;
     if ((e = init_variant<3, true, false>()) != cudaSuccess) return e;
+    if ((e = init_variant<2, false, true, true>()) != cudaSuccess) return e;
+    if ((e = init_variant<3, false, true, true>()) != cudaSuccess) return e;
+    if ((e = init_variant<2, false, false, true>()) != cudaSuccess) return e;
+    if ((e = init_variant<3, false, false, true>()) != cudaSuccess) return e;
     int nb = 0;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs_small<3, false, true>, kPairThreads, 0)) != cudaSuccess) return e;
     g_blocks_small = nb > 0 ? nb : 1;
@@ -1507,19 +1751,27 @@ cudaError_t launch_expand(const Params& p, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-template <int D, bool B, bool N>
+template <int D, bool B, bool N, bool R = false>
 static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st, cudaEvent_t* ev, unsigned evf) {
-    k_pairs_small<D, B, N><<<sm_count * g_blocks_small, kPairThreads, 0, st>>>(p);
+    k_pairs_small<D, B, N, R><<<sm_count * g_blocks_small, kPairThreads, 0, st>>>(p);
     if (ev) cudaEventRecordWithFlags(ev[0], st, evf);
-    k_pairs_med<D, B, N><<<sm_count * g_blocks_med, kPairThreads, med_smem(), st>>>(p);
+    k_pairs_med<D, B, N, R><<<sm_count * g_blocks_med, kPairThreads, med_smem(), st>>>(p);
     if (ev) cudaEventRecordWithFlags(ev[1], st, evf);
-    k_pairs_block<D, B, N><<<sm_count * g_blocks_block, kPairThreads, sizeof(BlockSmem), st>>>(p);
+    k_pairs_block<D, B, N, R><<<sm_count * g_blocks_block, kPairThreads, sizeof(BlockSmem), st>>>(p);
+    if (R) k_strip_entries<<<(unsigned)(sm_count * 4), 512, 0, st>>>(p);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev, unsigned evf) {
     const bool bip = p.split != kNoSplit;
     const bool narrow = p.max_range <= (1u << kMissShift);
+    if (p.records) {  // record mode: self queries
+        if (bip) return cudaErrorInvalidValue;
+        if (narrow) return dims == 2 ? launch_pairs_t<2, false, true, true>(p, sm_count, st, ev, evf)
+                                     : launch_pairs_t<3, false, true, true>(p, sm_count, st, ev, evf);
+        return dims == 2 ? launch_pairs_t<2, false, false, true>(p, sm_count, st, ev, evf)
+                         : launch_pairs_t<3, false, false, true>(p, sm_count, st, ev, evf);
+    }
     if (narrow) {
         if (dims == 2) return bip ? launch_pairs_t<2, true, true>(p, sm_count, st, ev, evf) : launch_pairs_t<2, false, true>(p, sm_count, st, ev, evf);
         return bip ? launch_pairs_t<3, true, true>(p, sm_count, st, ev, evf) : launch_pairs_t<3, false, true>(p, sm_count, st, ev, evf);

@@ -16,7 +16,8 @@ enum : uint32_t {
     kErrWait = 32u,       // a bounded spin-wait gave up
     kErrTaskOvf = 64u,    // tile-task buffer too small
     kErrCellOvf = 128u,   // one box covers >= 2^31 cells
-    kErrIndex = 256u      // more than 2^29 boxes in one launch
+    kErrIndex = 256u,     // more than 2^29 boxes in one launch
+    kErrRecCell = 512u    // record mode: a cell of 65536 boxes or more (the record format's limit)
 };
 
 constexpr uint32_t kNoSplit = 0xffffffffu;
@@ -56,6 +57,7 @@ struct Ctr {
     unsigned long long tests;           // sum of n(n-1)/2 over cells
     unsigned long long comp_pairs;      // sum of n*n/2 over cells of n >= 2 (the reference's numCompPairs)
     unsigned long long jobs;            // sum of ceil(n/256) over cells of n >= 2 (its 256-row jobs)
+    unsigned long long rec_pairs;       // record mode: pairs in the records (pairs counts 8-byte words)
 };
 
 // query sizes read from device memory (graph replays: one captured graph
@@ -90,6 +92,8 @@ struct Params {
     Ctr* ctr;
     const RunDims* dyn;           // when set, overrides nboxes / ncells / nscenes
     const uint32_t* merged;       // merged mode (one scene): cell -> root of its merged block, or kUnmerged
+    uint32_t records;             // record mode: work lists hold {cell id, n}; the pair kernels write the
+                                  // reference's Rice record stream (8-byte words) instead of pairs
 };
 
 constexpr uint32_t kUnmerged = 0x0fffff11u;  // a cell outside every merged block

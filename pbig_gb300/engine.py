@@ -31,6 +31,7 @@ EXPORTS = [
     "pbig2_host_free", "pbig2_get_stats", "pbig2_tune_shift", "pbig2_self_intersect_noalloc",
     "pbig2_noalloc_last_error", "pbig2_set_option", "pbig2_scene_create", "pbig2_scene_destroy",
     "pbig2_scene_move", "pbig2_scene_delta", "pbig2_scene_pairs", "pbig2_scene_boxes", "pbig2_scene_copy",
+    "pbig2_result_records", "pbig2_copy_records", "pbig2_decode_records",
 ]
 
 
@@ -83,6 +84,10 @@ def lib():
         L.pbig2_scene_move.argtypes = [vp, vp, u64, vp, C.c_int, C.POINTER(u64), C.POINTER(u64)]
         L.pbig2_scene_copy.argtypes = [vp, C.c_int, vp, u64]
         L.pbig2_scene_pairs.argtypes = [vp, C.POINTER(vp), C.POINTER(u64)]
+        L.pbig2_result_records.argtypes = [vp, C.POINTER(vp), C.POINTER(u64), C.POINTER(vp), C.POINTER(u64),
+                                           C.POINTER(vp), C.POINTER(u64)]
+        L.pbig2_copy_records.argtypes = [vp, vp, vp, vp]
+        L.pbig2_decode_records.argtypes = [vp, u64, vp, u64, vp, u64, vp, u64, C.POINTER(u64)]
         L.pbig2_result_scene_offsets.argtypes = [vp, C.POINTER(u64), u32]
         L.pbig2_get_stats.argtypes = [vp, C.POINTER(Stats)]
         L.pbig2_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
@@ -267,6 +272,25 @@ class Engine:
         build's work statistics)."""
         _check(self._L.pbig2_set_option(self._ctx, 2, int(bool(on))))
 
+    def set_records(self, on: bool) -> None:
+        """Self queries return the reference's Rice record stream (PBIG2_OPT_RICE)."""
+        _check(self._L.pbig2_set_option(self._ctx, 3, int(bool(on))))
+
+    def records(self):
+        """(words uint64, StartI uint32, Recs uint32) of the last record-mode
+        query, copied to the host."""
+        vp = C.c_void_p
+        w, si, rc = vp(), vp(), vp()
+        nw, nc, ne = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(self._L.pbig2_result_records(self._ctx, C.byref(w), C.byref(nw), C.byref(si), C.byref(nc),
+                                            C.byref(rc), C.byref(ne)))
+        words = np.empty(nw.value, dtype=np.uint64)
+        start_i = np.empty(nc.value, dtype=np.uint32)
+        recs = np.empty(ne.value, dtype=np.uint32)
+        _check(self._L.pbig2_copy_records(self._ctx, vp(words.ctypes.data), vp(start_i.ctypes.data),
+                                          vp(recs.ctypes.data)))
+        return words, start_i, recs
+
     def set_graphs(self, on: bool) -> None:
         """Capture/replay batched queries as CUDA graphs (on by default)."""
         _check(self._L.pbig2_set_option(self._ctx, 1, int(bool(on))))
@@ -275,6 +299,21 @@ class Engine:
         s = Stats()
         _check(self._L.pbig2_get_stats(self._ctx, C.byref(s)))
         return s.as_dict()
+
+
+def decode_records(words: np.ndarray, start_i: np.ndarray, recs: np.ndarray) -> np.ndarray:
+    """pbig2_decode_records: a Rice record stream (host arrays) -> [P,2] pairs."""
+    L = lib()
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    si = np.ascontiguousarray(start_i, dtype=np.uint32)
+    rc = np.ascontiguousarray(recs, dtype=np.uint32)
+    n = C.c_uint64()
+    vp = C.c_void_p
+    args = (vp(w.ctypes.data), w.shape[0], vp(si.ctypes.data), si.shape[0], vp(rc.ctypes.data), rc.shape[0])
+    _check(L.pbig2_decode_records(*args, None, 0, C.byref(n)), (OK, ECAPACITY))
+    out = np.empty((n.value, 2), dtype=np.uint32)
+    _check(L.pbig2_decode_records(*args, vp(out.ctypes.data), n.value, C.byref(n)))
+    return out
 
 
 class Scene:
