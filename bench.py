@@ -581,7 +581,7 @@ def run_serving(args, rank, local, ws):
     srv.close()
     # pairs are delivered into each slot's page-locked host buffer (the
     # device->host copy is timed; no second host copy)
-    srv = serve.Server(device=local, budget_bytes=40 << 30, copy_pairs=False)
+    srv = serve.Server(device=local, budget_bytes=40 << 30, copy_pairs=False, reserve_boxes=4 << 20)
     with ClockSampler(local) as clk:
         th = serve.feed(srv, reqs)
         srv.serve(len(reqs))
@@ -592,7 +592,7 @@ def run_serving(args, rank, local, ws):
         "metric": METRIC + " (serving p50/p99)", "value": s["p99_ms"], "unit": "ms (p99 latency)", "n_gpus": ws,
         "steps": len(reqs), "warmup": len(warm), "ms_per_step": s["mean_ms"], "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"serving: Poisson arrivals at {args.rate:.0f} req/s for {args.duration} s, 30% updates moving 1% of a resident scene's boxes by N(0,0.001), new scenes log-uniform in [1024, 1048576] boxes, 40 GB device budget, 2 slots",
+        "config": {"workload": f"serving: Poisson arrivals at {args.rate:.0f} req/s for {args.duration} s, 30% updates moving 1% of a resident scene's boxes by N(0,0.001), new scenes log-uniform in [1024, 1048576] boxes, 40 GB device budget, 2 slots, capacity for 4,194,304-box batches reserved at start",
                    "requests": len(reqs), "updates": sum(r.kind == "update" for r in reqs),
                    "mean_scene_boxes": float(np.mean(sizes)), "parallelism": "single GPU"},
         "latency_ms": {"p50": s["p50_ms"], "p99": s["p99_ms"], "mean": s["mean_ms"], "max": s["max_ms"]},
@@ -601,6 +601,10 @@ def run_serving(args, rank, local, ws):
         "gpu_slot_busy_fraction": srv.busy_time / max(1e-9, s["span_s"]) / len(srv.engines),
         "evictions": srv.evictions, "refused": srv.refused,
         "host_ms_per_batch": {k: v * 1e3 / max(1, srv.batches) for k, v in srv.phase_s.items()},
+        "slowest_batches": [{"start_s": round(b[0], 4), "boxes": b[1], "requests": b[2],
+                             "phase_ms": [round(x, 3) for x in b[3:7]],
+                             "prepare_split_ms": [round(x, 3) for x in b[7:]]}
+                            for b in sorted(srv.batch_log, key=lambda b: -sum(b[3:7]))[:5]],
         "clocks": clk.summary(),
     }
     srv.close()

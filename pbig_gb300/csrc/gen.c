@@ -275,31 +275,15 @@ double pbig_gen_normal(uint64_t seed, uint64_t stream, uint64_t idx) {
     return normal(seed, stream, idx);
 }
 
-static uint64_t gcd64(uint64_t a, uint64_t b) {
-    while (b) { uint64_t t = a % b; a = b; b = t; }
-    return a;
-}
-
-static int cmp_u32(const void* a, const void* b) {
-    uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
-    return x < y ? -1 : x > y;
-}
-
-/* k distinct indices in [0, n), sorted: the arithmetic progression
- * start + j*step (mod n), j < k, with start and step drawn from the seed and
- * step coprime to n (so the k values are distinct). */
+/* k distinct indices in [0, n), sorted: one per stratum -- index j is drawn
+ * uniformly from [j*n/k, (j+1)*n/k) -- so no sort is needed. */
 int pbig_gen_pick(uint64_t n, uint64_t k, uint64_t seed, uint32_t* out) {
-    if (n == 0 || k > n) return -1;
-    uint64_t start = rng_u64(seed, S_PICK, 0) % n;
-    uint64_t step = n > 1 ? 1 + rng_u64(seed, S_PICK, 1) % (n - 1) : 1;
-    for (uint64_t t = 2; gcd64(step, n) != 1; t++) step = 1 + rng_u64(seed, S_PICK, t) % (n - 1);
-    uint64_t x = start;
+    if (n == 0 || k == 0 || k > n) return -1;
     for (uint64_t j = 0; j < k; j++) {
-        out[j] = (uint32_t)x;
-        x += step;
-        if (x >= n) x -= n;
+        const uint64_t lo = (uint64_t)(((unsigned __int128)j * n) / k);
+        const uint64_t hi = (uint64_t)(((unsigned __int128)(j + 1) * n) / k);
+        out[j] = (uint32_t)(lo + rng_u64(seed, S_PICK, j) % (hi - lo));
     }
-    qsort(out, k, sizeof(uint32_t), cmp_u32);
     return 0;
 }
 
@@ -340,8 +324,7 @@ static inline double normal_nodiv(uint64_t seed, uint64_t stream, uint64_t idx) 
     return sqrt(-2.0 * log_nodiv(u1)) * cos2pi_nodiv(u2);
 }
 
-int pbig_gen_move3d(uint32_t* boxes, const uint32_t* idx, uint64_t k, uint64_t seed,
-                    double sigma) {
+int pbig_gen_move3d(uint32_t* boxes, const uint32_t* idx, uint64_t k, uint64_t seed, double sigma) {
     for (uint64_t t = 0; t < k; t++) {
         uint32_t* b = boxes + (uint64_t)idx[t] * 7;
         double lo[3], hi[3];

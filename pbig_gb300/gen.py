@@ -117,8 +117,8 @@ def move3d(boxes: np.ndarray, idx: np.ndarray, seed: int, sigma: float = 0.001) 
 
 
 def pick(n: int, k: int, seed: int) -> np.ndarray:
-    """k distinct sorted indices in [0, n) (seeded arithmetic progression with
-    a step coprime to n)."""
+    """k distinct sorted indices in [0, n): one drawn uniformly from each of
+    k equal strata (seeded)."""
     out = np.empty(k, dtype=np.uint32)
     if _lib().pbig_gen_pick(n, k, seed, _p(out)) != 0:
         raise ValueError("need 0 < k <= n")

@@ -21,6 +21,8 @@ concurrently.
 from __future__ import annotations
 
 import collections
+import gc
+import sys
 import threading
 import time
 from dataclasses import dataclass, field
@@ -44,6 +46,8 @@ class Request:
     move_frac: float = 0.01    # update: fraction of boxes moved
     move_seed: int = 0
     move_sigma: float = 0.001
+    idx: np.ndarray | None = None       # update: indices of the moved boxes (sorted, distinct)
+    rows: np.ndarray | None = None      # update: their new RectInfo rows
     # filled by the server
     start: float = 0.0
     done: float = 0.0
@@ -54,6 +58,46 @@ class Request:
     nboxes: int = 0
 
 
+class _Arena:
+    """First-fit allocator over one device allocation of int32 words: the
+    resident scenes live in it, so uploading a scene never calls cudaMalloc
+    (which blocks the whole device) while requests wait. Blocks are rounded
+    to 64 words (256 bytes)."""
+
+    def __init__(self, torch, words: int, device: int):
+        self.buf = torch.empty(max(64, words), dtype=torch.int32, device=f"cuda:{device}")
+        self.free = [(0, self.buf.shape[0])]  # (offset, length), sorted by offset
+
+    @staticmethod
+    def _round(words: int) -> int:
+        return (words + 63) & ~63
+
+    def alloc(self, words: int):
+        w = self._round(words)
+        for i, (off, ln) in enumerate(self.free):
+            if ln >= w:
+                if ln == w:
+                    del self.free[i]
+                else:
+                    self.free[i] = (off + w, ln - w)
+                return off
+        return None
+
+    def release(self, off: int, words: int) -> None:
+        w = self._round(words)
+        i = 0
+        while i < len(self.free) and self.free[i][0] < off:
+            i += 1
+        self.free.insert(i, (off, w))
+        # coalesce with the neighbours
+        if i + 1 < len(self.free) and self.free[i][0] + self.free[i][1] == self.free[i + 1][0]:
+            self.free[i] = (off, self.free[i][1] + self.free[i + 1][1])
+            del self.free[i + 1]
+        if i > 0 and self.free[i - 1][0] + self.free[i - 1][1] == self.free[i][0]:
+            self.free[i - 1] = (self.free[i - 1][0], self.free[i - 1][1] + self.free[i][1])
+            del self.free[i]
+
+
 @dataclass
 class Scene:
     sid: int
@@ -62,6 +106,7 @@ class Scene:
     shift: int
     last_used: float = 0.0
     busy: bool = False
+    arena_off: int | None = None  # where dev lives in the server's arena
 
     @property
     def bytes(self) -> int:
@@ -71,7 +116,7 @@ class Scene:
 class Server:
     def __init__(self, device: int = 0, budget_bytes: int = 40 << 30, slots: int = 2,
                  max_batch_boxes: int = 64 << 20, keep_pairs: bool = True, keep_snapshots: bool = False,
-                 copy_pairs: bool = True):
+                 copy_pairs: bool = True, reserve_boxes: int = 0):
         import torch
         self.torch = torch
         self.device = device
@@ -92,15 +137,37 @@ class Server:
         # each slot orders its uploads and its batch on its own stream, and
         # downloads pairs into its own page-locked buffer
         self.streams = [torch.cuda.Stream(device=device) for _ in range(slots)]
-        self.pinned = [torch.empty((1 << 20, 2), dtype=torch.int32).pin_memory() for _ in range(slots)]
+        # capacity reserved up front: a synthetic batch of reserve_boxes boxes
+        # (four scenes) through every slot grows its engine buffers, and the
+        # page-locked pair buffers start at twice as many pairs, so batches up
+        # to that size allocate nothing (no cudaMalloc / cudaHostAlloc while
+        # requests wait)
+        pairs0 = max(1 << 20, 2 * reserve_boxes)
+        self.pinned = [torch.empty((pairs0, 2), dtype=torch.int32).pin_memory() for _ in range(slots)]
+        # per-slot device buffer the batch's scenes are concatenated into
+        self.catbuf = [torch.empty((max(reserve_boxes, 1 << 16), 7), dtype=torch.int32, device=f"cuda:{device}")
+                       for _ in range(slots)]
+        self.arena = _Arena(torch, budget_bytes // 4, device)
+        if reserve_boxes:
+            q = reserve_boxes // 4
+            parts = [gen.scene3d(q, 424242 + k) for k in range(4)]
+            offs = np.array([0, q, 2 * q, 3 * q, 4 * q], dtype=np.uint64)
+            boxes = torch.from_numpy(np.concatenate(parts).view(np.int32)).to(f"cuda:{device}")
+            shifts = np.array([tune_shift(b, gen.RANGE, 256) for b in parts], dtype=np.uint32)
+            for e, st in zip(self.engines, self.streams):
+                e.batch_intersect(boxes, offs, gen.RANGE, cell_shifts=shifts, stream=st)
+                e.sync(st)
+            del boxes
         self.staging = [torch.empty((1 << 16, 8), dtype=torch.int32).pin_memory() for _ in range(slots)]
         self.free_slots = list(range(slots))
         self.batches = 0
+        gc.collect()  # before the clock starts: serve() runs with the collector paused
         self.t0 = time.perf_counter()
         self.busy_time = 0.0
         self.evictions = 0
         self.refused = 0
         self.phase_s = collections.defaultdict(float)  # host seconds per batch phase (summed)
+        self.batch_log: list[tuple] = []  # (start s, boxes, requests, prepare, concat, query, download ms)
 
     # ---- request intake -------------------------------------------------
     def now(self) -> float:
@@ -123,10 +190,39 @@ class Server:
                     break
             if victim is None:
                 return False
-            victim.dev = None
-            self.resident_bytes -= victim.bytes
-            self.evictions += 1
+            self._drop(victim)
         return True
+
+    def _drop(self, sc: Scene) -> None:
+        """Forget a scene's device copy (its host copy stays)."""
+        if sc.arena_off is not None:
+            self.arena.release(sc.arena_off, sc.host.size)
+            sc.arena_off = None
+        sc.dev = None
+        self.resident_bytes -= sc.bytes
+        self.evictions += 1
+
+    def _upload(self, sc: Scene, dev: str) -> None:
+        """Copy a scene to the device: into the arena (evicting idle scenes,
+        least recently used first, when it is too fragmented), else through
+        the caching allocator."""
+        torch = self.torch
+        src = torch.from_numpy(sc.host.view(np.int32))
+        with self.lock:
+            off = self.arena.alloc(sc.host.size)
+            while off is None:
+                victim = next((v for v in self.scenes.values()
+                               if v.dev is not None and not v.busy and v.arena_off is not None), None)
+                if victim is None:
+                    break
+                self._drop(victim)
+                off = self.arena.alloc(sc.host.size)
+        if off is None:
+            sc.dev = src.to(dev, non_blocking=True)
+            return
+        sc.arena_off = off
+        sc.dev = self.arena.buf[off:off + sc.host.size].view(sc.host.shape[0], 7)
+        sc.dev.copy_(src, non_blocking=True)
 
     def _take_batch(self) -> list[Request]:
         """Pending requests that can run now (caller holds the lock)."""
@@ -183,12 +279,17 @@ class Server:
         stream = self.streams[slot]
         tp = [time.perf_counter()]
         with torch.cuda.stream(stream):
-            self._prepare(batch, scenes, dev, slot)
+            prep_split = self._prepare(batch, scenes, dev, slot)
             tp.append(time.perf_counter())
             offs = np.zeros(len(batch) + 1, dtype=np.uint64)
             for i, sc in enumerate(scenes):
                 offs[i + 1] = offs[i] + sc.host.shape[0]
-            cat = torch.cat([sc.dev for sc in scenes]) if len(scenes) > 1 else scenes[0].dev
+            if len(scenes) == 1:
+                cat = scenes[0].dev
+            elif int(offs[-1]) <= self.catbuf[slot].shape[0]:
+                cat = torch.cat([sc.dev for sc in scenes], out=self.catbuf[slot][:int(offs[-1])])
+            else:
+                cat = torch.cat([sc.dev for sc in scenes])
             shifts = np.array([sc.shift for sc in scenes], dtype=np.uint32)
             tp.append(time.perf_counter())
             total = eng.batch_intersect(cat, offs, gen.RANGE, cell_shifts=shifts, stream=stream)
@@ -215,6 +316,9 @@ class Server:
             for k, name in enumerate(("prepare", "concat", "query", "download")):
                 if k + 1 < len(tp):
                     self.phase_s[name] += tp[k + 1] - tp[k]
+            self.batch_log.append((t_start, sum(r.nboxes for r in batch), len(batch),
+                                   *[(tp[k + 1] - tp[k]) * 1e3 for k in range(len(tp) - 1)],
+                                   *[x * 1e3 for x in prep_split]))
             self.batches += 1
             self.busy_time += t_done - t_start
             for sc in scenes:
@@ -232,19 +336,28 @@ class Server:
         again: the slot's previous batch ended with a stream synchronize)."""
         torch = self.torch
         moved = []  # (scene, indices) of updates whose scene stays resident
+        tt = [0.0, 0.0, 0.0, 0.0]  # host seconds: tuning, update rows, uploads, moved rows
         for r, sc in zip(batch, scenes):
             r.nboxes = sc.host.shape[0]
+            t0 = time.perf_counter()
             if sc.shift < 0:  # first query of the scene: tune its cell size once
                 sc.shift = tune_shift(sc.host, gen.RANGE, 256)
-            if r.kind == "update":  # move a fraction of the boxes (host master copy)
-                idx = move_indices(sc.host.shape[0], r.move_frac, r.move_seed)
-                gen.move3d(sc.host, idx, r.move_seed, r.move_sigma)
+            t1 = time.perf_counter()
+            if r.kind == "update":  # the moved rows replace theirs in the host master copy
+                idx = r.idx
+                sc.host[idx] = r.rows
                 if sc.dev is not None:
                     moved.append((sc, idx))
+            t2 = time.perf_counter()
             if sc.dev is None:  # not on the device (new or dropped): upload it whole
-                sc.dev = torch.from_numpy(sc.host.view(np.int32)).to(dev, non_blocking=True)
+                self._upload(sc, dev)
+            t3 = time.perf_counter()
+            tt[0] += t1 - t0
+            tt[1] += t2 - t1
+            tt[2] += t3 - t2
             if self.keep_snapshots:
                 r.snapshot = sc.host.copy()
+        t4 = time.perf_counter()
         if moved:
             k = sum(idx.shape[0] for _, idx in moved)
             if self.staging[slot].shape[0] < k:
@@ -262,10 +375,30 @@ class Server:
                 b = a + idx.shape[0]
                 sc.dev.index_copy_(0, up[a:b, 7].long(), up[a:b, :7])
                 a = b
+        tt[3] = time.perf_counter() - t4
+        return tt
 
     # ---- dispatcher ----------------------------------------------------------
     def serve(self, n_expected: int, timeout: float = 600.0) -> None:
-        """Dispatch until n_expected requests have completed (or were refused)."""
+        """Dispatch until n_expected requests have completed (or were refused).
+
+        While it runs, the interpreter switches threads every 0.2 ms (not the
+        default 5 ms: a slot thread waiting for the GIL would add that to a
+        request's latency) and the cyclic garbage collector is paused (the
+        constructor collected once), so no collection pause lands in the
+        middle of a batch; both are restored on return."""
+        switch = sys.getswitchinterval()
+        gc_on = gc.isenabled()
+        gc.disable()
+        sys.setswitchinterval(min(switch, 0.0002))
+        try:
+            self._serve(n_expected, timeout)
+        finally:
+            sys.setswitchinterval(switch)
+            if gc_on:
+                gc.enable()
+
+    def _serve(self, n_expected: int, timeout: float) -> None:
         threads = []
         deadline = time.perf_counter() + timeout
         while True:
@@ -309,8 +442,12 @@ def make_requests(duration: float, rate: float = 2000.0, seed: int = 0, lo: int 
     """Seeded request stream: Poisson arrivals, `update_frac` of them updates
     of an earlier scene (uniform over the scenes queried before), the rest
     queries of new scenes with log-uniform sizes in [lo, hi] (the batched
-    scenes' generator)."""
+    scenes' generator). An update carries the indices and new rows of the
+    moved boxes, as a client that owns its scene would send them: the
+    clients' copies of the scenes are moved here, in arrival order."""
     reqs, t, i, scene_ids = [], 0.0, 0, []
+    client: dict[int, np.ndarray] = {}  # scene -> the client's current boxes
+    first_req: dict[int, int] = {}      # scene -> its query request
     while True:
         u = gen.uniform(seed, 20, i)
         t += -np.log(1.0 - u) / rate
@@ -318,11 +455,19 @@ def make_requests(duration: float, rate: float = 2000.0, seed: int = 0, lo: int 
             break
         if scene_ids and gen.uniform(seed, 21, i) < update_frac:
             sid = scene_ids[int(gen.uniform(seed, 22, i) * len(scene_ids))]
-            reqs.append(Request(i, t, sid, "update", move_frac=move_frac, move_seed=seed * 1000003 + i))
+            r = Request(i, t, sid, "update", move_frac=move_frac, move_seed=seed * 1000003 + i)
+            if sid not in client:
+                client[sid] = reqs[first_req[sid]].boxes.copy()
+            cur = client[sid]
+            r.idx = move_indices(cur.shape[0], r.move_frac, r.move_seed)
+            gen.move3d(cur, r.idx, r.move_seed, r.move_sigma)
+            r.rows = cur[r.idx]
+            reqs.append(r)
         else:
             n = int(gen.scene_sizes(1, seed * 7919 + i, lo, hi)[0])
             sid = len(scene_ids)
             scene_ids.append(sid)
+            first_req[sid] = len(reqs)
             out = pinned_boxes(n) if pinned else None
             reqs.append(Request(i, t, sid, "query", boxes=gen.scene3d(n, seed=seed * 1000003 + i, out=out)))
         i += 1
