@@ -198,6 +198,13 @@ PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
  * written (PBIG2_ECAPACITY). Blocks are per emission step, so one cell can
  * have several (as the reference's cells of several jobs do). */
 #define PBIG2_OPT_RICE 3
+/* PBIG2_OPT_HOST_SPLIT (default 0 = automatic): when the pair output set by
+ * pbig2_set_pair_output is page-locked host memory, the pair phase is bound
+ * by the host link; the small-cell and block kernels then run on their own
+ * stream over this many SMs (automatic: a quarter) beside the medium-cell
+ * kernel on the rest, so the link is not idle while they compute. A
+ * negative value runs the three kernels one after another. */
+#define PBIG2_OPT_HOST_SPLIT 4
 PBIG2_API int pbig2_set_option(pbig2_ctx* ctx, int option, int64_t value);
 
 /* Allocation-free self-intersection (no counterpart in the reference).

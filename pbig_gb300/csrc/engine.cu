@@ -289,7 +289,12 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
         R(cudaMemsetAsync(&p.ctr->err, 0, sizeof(unsigned int), st));
         R(cudaEventRecordWithFlags(c->evp[4], st, evf));
     }
-    R(launch_pairs(p, dims, c->sm_count, st, &c->evp[7], evf));  // records evp[7], evp[8]
+    // pairs stored over the host link: the lighter pair kernels run beside
+    // the medium-cell kernel (two fifths of the SMs unless set)
+    PairOverlap ov{c->side_stream, c->ev_fork, c->ev_join,
+                   c->host_split > 0 ? c->host_split : (2 * c->sm_count + 2) / 5};
+    const bool overlap = c->ext_host && p.out == c->ext_out && c->host_split >= 0 && !p.records;
+    R(launch_pairs(p, dims, c->sm_count, st, &c->evp[7], evf, overlap ? &ov : nullptr));  // records evp[7], evp[8]
     R(cudaEventRecordWithFlags(c->evp[5], st, evf));
     if (grouped) {
         unsigned long long* hist = c->d_scene_cursor.as<unsigned long long>();
@@ -333,9 +338,11 @@ static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t nc
     {
         float x = 0;
         if (grouped && cudaEventElapsedTime(&x, c->evp[5], c->ev1) == cudaSuccess) phase[5] = x;
-        if (cudaEventElapsedTime(&x, c->evp[4], c->evp[7]) == cudaSuccess) phase[6] = x;
-        if (cudaEventElapsedTime(&x, c->evp[7], c->evp[8]) == cudaSuccess) phase[7] = x;
-        if (cudaEventElapsedTime(&x, c->evp[8], c->evp[5]) == cudaSuccess) phase[8] = x;
+        // (the pair kernels may overlap: a phase that ends before the
+        // previous one reads 0)
+        if (cudaEventElapsedTime(&x, c->evp[4], c->evp[7]) == cudaSuccess) phase[6] = std::max(0.f, x);
+        if (cudaEventElapsedTime(&x, c->evp[7], c->evp[8]) == cudaSuccess) phase[7] = std::max(0.f, x);
+        if (cudaEventElapsedTime(&x, c->evp[8], c->evp[5]) == cudaSuccess) phase[8] = std::max(0.f, x);
     }
     pbig2_stats& s = c->stats;
     s.boxes = nboxes;
@@ -571,6 +578,12 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     Params p{};
     p.boxes = d_boxes;
     p.nboxes = nboxes;
+    if (c->up_red || c->up_blue) {  // the count uploads the boxes (self and red/blue queries)
+        p.up_red = c->up_red;
+        p.up_blue = c->up_blue;
+        p.up_split = c->up_split;
+        p.box_copy = const_cast<uint32_t*>(d_boxes);
+    }
     p.scenes = c->d_scenes.as<Scene>();
     p.scene_box_off = c->d_scene_off.as<uint32_t>();
     p.nscenes = nsc;
@@ -689,6 +702,16 @@ static int sample_device_boxes(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t n
     return PBIG2_OK;
 }
 
+// device-mapped address of page-locked host memory, or null (pageable memory)
+static const uint32_t* mapped_host(const uint32_t* h) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? static_cast<const uint32_t*>(a.devicePointer) : nullptr;
+}
+
 static int stage_boxes_in(pbig2_ctx* c, const uint32_t* boxes, uint64_t words, int loc, cudaStream_t st,
                           const uint32_t** d_boxes) {
     if (loc == PBIG2_DEVICE) {
@@ -725,6 +748,9 @@ PBIG2_API int pbig2_create(int device, pbig2_ctx** out) {
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     for (int k = 0; k < 9 && e == cudaSuccess; k++) e = cudaEventCreate(&c->evp[k]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = kernels_init();
     if (e != cudaSuccess) {
         pbig2_destroy(c);
@@ -750,6 +776,9 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (cudaEvent_t ev : c->evp)
         if (ev) cudaEventDestroy(ev);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side_stream) cudaStreamDestroy(c->side_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return PBIG2_OK;
@@ -797,7 +826,15 @@ static int self_or_bip(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const 
     const bool bip = blue != nullptr;
     const uint64_t n = n_red + n_blue;
     const uint32_t* d_boxes = nullptr;
-    if (!bip) {
+    // page-locked host input needs no copy before the pipeline: the count
+    // kernel reads it over the host link and writes the device copy
+    const uint32_t* m_red = loc == PBIG2_HOST && n_red ? mapped_host(red) : nullptr;
+    const uint32_t* m_blue = loc == PBIG2_HOST && bip && n_blue ? mapped_host(blue) : nullptr;
+    const bool fused = loc == PBIG2_HOST && n > 0 && (n_red == 0 || m_red) && (!bip || n_blue == 0 || m_blue);
+    if (fused) {
+        CK(c->d_boxes.ensure(n * W * 4 + 16, false, st));
+        d_boxes = c->d_boxes.as<uint32_t>();
+    } else if (!bip) {
         int rc = stage_boxes_in(c, red, n_red * W, loc, st, &d_boxes);
         if (rc) return rc;
     } else {
@@ -837,8 +874,14 @@ static int self_or_bip(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const 
         sc.push_back({0, n_red, tr.shift, 0});
         sc.push_back({n_red, n_blue, tr.shift, 0});
     }
+    if (fused) {
+        c->up_red = m_red;
+        c->up_blue = m_blue;
+        c->up_split = n_red;
+    }
     int rc = run_pipeline(c, d_boxes, n, (int)dims, range, sc, bip ? (uint32_t)n_red : kNoSplit,
                           std::max(tr.est_entries, (double)n), st, false);
+    c->up_red = c->up_blue = nullptr;
     *npairs = c->npairs;
     return rc;
 }
@@ -1033,8 +1076,10 @@ PBIG2_API int pbig2_set_pair_output(pbig2_ctx* c, uint32_t* dst, uint64_t cap_pa
         }
         if (((uintptr_t)dst & 7u) != 0) return fail(PBIG2_EINVAL, "pair output must be 8-byte aligned");
         c->ext_out = reinterpret_cast<uint2*>(a.devicePointer);
+        c->ext_host = a.type == cudaMemoryTypeHost;
     } else {
         c->ext_out = nullptr;
+        c->ext_host = false;
     }
     c->ext_cap = dst ? cap_pairs : 0;
     return PBIG2_OK;
@@ -1080,6 +1125,12 @@ PBIG2_API int pbig2_set_option(pbig2_ctx* c, int option, int64_t value) {
     }
     if (option == PBIG2_OPT_RICE) {
         c->rice_mode = value != 0;
+        return PBIG2_OK;
+    }
+    if (option == PBIG2_OPT_HOST_SPLIT) {
+        if (value >= c->sm_count) return fail(PBIG2_EINVAL, "host split of %lld SMs (the device has %d)",
+                                              (long long)value, c->sm_count);
+        c->host_split = value < 0 ? -1 : (int)value;
         return PBIG2_OK;
     }
     return fail(PBIG2_EINVAL, "unknown option %d", option);

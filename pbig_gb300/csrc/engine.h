@@ -66,6 +66,17 @@ struct pbig2_ctx {
     // caller's pair buffer for self/bipartite queries (pbig2_set_pair_output)
     uint2* ext_out = nullptr;
     uint64_t ext_cap = 0;
+    bool ext_host = false;    // ext_out is page-locked host memory
+    // pairs to host memory: SMs of the small-cell and block kernels beside
+    // the medium-cell kernel (PBIG2_OPT_HOST_SPLIT; 0 = automatic, < 0 = off)
+    int host_split = 0;
+    cudaStream_t side_stream = nullptr;
+    // page-locked host input of the running query, uploaded by the count
+    // kernel (device-mapped addresses; null: the boxes are on the device)
+    const uint32_t* up_red = nullptr;
+    const uint32_t* up_blue = nullptr;
+    uint64_t up_split = 0;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool result_ext = false;  // the last result went to ext_out
     // last result
     const uint2* result = nullptr;

@@ -89,6 +89,43 @@ __device__ __forceinline__ void stage_boxes(const Params& p, uint64_t b0, uint32
     }
 }
 
+__device__ __forceinline__ void copy_words(const uint32_t* src, uint32_t* dst, uint32_t nwords) {
+    if ((((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) && (nwords & 3u) == 0) {
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+        for (uint32_t k = threadIdx.x; k < nwords / 4; k += blockDim.x) d4[k] = __ldg(s4 + k);
+    } else {
+        for (uint32_t k = threadIdx.x; k < nwords; k += blockDim.x) dst[k] = __ldg(src + k);
+    }
+}
+
+// the count's upload: a tile of boxes from page-locked host memory into
+// shared memory (the host link is the bound, so the count's own work hides
+// under it), then on to the device copy
+template <int D>
+__device__ __forceinline__ void stage_upload(const Params& p, uint64_t b0, uint32_t nb, uint32_t* sbox) {
+    constexpr uint32_t W = 2 * D + 1;
+    const uint64_t split = p.up_split;
+    if (b0 + nb <= split || b0 >= split) {
+        copy_words(b0 < split ? p.up_red + b0 * W : p.up_blue + (b0 - split) * W, sbox, nb * W);
+    } else {  // the tile straddles red and blue
+        const uint64_t sw = split * W;
+        for (uint32_t k = threadIdx.x; k < nb * W; k += blockDim.x) {
+            const uint64_t gw = b0 * W + k;
+            sbox[k] = gw < sw ? __ldg(p.up_red + gw) : __ldg(p.up_blue + (gw - sw));
+        }
+    }
+    __syncthreads();
+    uint32_t* dst = p.box_copy + b0 * W;
+    if (((reinterpret_cast<uintptr_t>(dst) & 15u) == 0) && ((nb * W) & 3u) == 0) {
+        const uint4* s4 = reinterpret_cast<const uint4*>(sbox);
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+        for (uint32_t k = threadIdx.x; k < nb * W / 4; k += blockDim.x) d4[k] = s4[k];
+    } else {
+        for (uint32_t k = threadIdx.x; k < nb * W; k += blockDim.x) dst[k] = sbox[k];
+    }
+}
+
 template <int D, bool SCATTER, bool MERGED>
 __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t* sbox, uint64_t b0,
                                                 uint32_t nb) {
@@ -201,7 +238,8 @@ __global__ void __launch_bounds__(kBoxThreads) k_count(Params pin) {
     const Params p = resolve(pin);
     for (uint64_t b0 = (uint64_t)blockIdx.x * kBoxThreads; b0 < p.nboxes; b0 += (uint64_t)gridDim.x * kBoxThreads) {
         const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
-        stage_boxes<D>(p, b0, nb, sbox);
+        if (p.box_copy) stage_upload<D>(p, b0, nb, sbox);
+        else stage_boxes<D>(p, b0, nb, sbox);
         __syncthreads();
         enumerate_cells<D, false, MERGED>(p, sbox, b0, nb);
         __syncthreads();
@@ -760,6 +798,38 @@ struct WarpOut {
     unsigned long long hits = 0;  // record mode: pairs written by this lane
 };
 
+// copy n pairs (8-byte words) from shared memory to p.out[base, base + n):
+// thread t of nt (a multiple of 32) stores 16-byte units laid on the
+// destination's 128-byte lines, so a warp store covers whole lines and only
+// the first and last line of a run are partial. The pair array may be
+// page-locked host memory, where partial lines cost a large share of the
+// link's write bandwidth.
+__device__ __forceinline__ void store_run(const Params& p, unsigned long long base, const uint2* src, uint32_t n,
+                                          uint32_t t, uint32_t nt) {
+    if (base + n > p.out_cap) {
+        for (uint32_t k = t; k < n; k += nt) {
+            const unsigned long long g = base + k;
+            if (g < p.out_cap) p.out[g] = src[k];
+            else atomicOr(&p.ctr->err, kErrOutOvf);
+        }
+        return;
+    }
+    // pairs of base's line before base (the pair array is 8-byte aligned)
+    const uint32_t lead = (uint32_t)(((reinterpret_cast<uintptr_t>(p.out) >> 3) + base) & 15u);
+    const uint32_t units = (lead + n + 1) >> 1;
+    uint2* dst = p.out + base;
+    for (uint32_t u = t; u < units; u += nt) {
+        const int r = 2 * (int)u - (int)lead;  // first pair of the unit, relative to base
+        if (r >= 0 && r + 1 < (int)n) {
+            const uint2 a = src[r], b = src[r + 1];
+            *reinterpret_cast<uint4*>(dst + r) = make_uint4(a.x, a.y, b.x, b.y);
+        } else {
+            if (r >= 0 && r < (int)n) dst[r] = src[r];
+            if (r + 1 >= 0 && r + 1 < (int)n) dst[r + 1] = src[r + 1];
+        }
+    }
+}
+
 __device__ __forceinline__ void wflush(const Params& p, WarpOut& o) {
     if (o.n == 0) return;
     const uint32_t lane = lane_id();
@@ -767,11 +837,7 @@ __device__ __forceinline__ void wflush(const Params& p, WarpOut& o) {
     if (lane == 0) base = atomicAdd(&p.ctr->pairs, (unsigned long long)o.n);
     base = __shfl_sync(FULL_MASK, base, 0);
     __syncwarp();
-    for (uint32_t k = lane; k < o.n; k += 32) {
-        const unsigned long long g = base + k;
-        if (g < p.out_cap) p.out[g] = o.buf[k];
-        else atomicOr(&p.ctr->err, kErrOutOvf);
-    }
+    store_run(p, base, o.buf, o.n, lane, 32);
     __syncwarp();
     o.n = 0;
 }
@@ -1520,12 +1586,7 @@ __global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
         if (nv >= kBlockOut / 2 || on > nv || (last && on > 0)) {
             if (t == 0) s.gbase = nv ? atomicAdd(&p.ctr->pairs, (unsigned long long)nv) : 0ull;
             __syncthreads();
-            const unsigned long long gb = s.gbase;
-            for (uint32_t k = t; k < nv; k += kPairThreads) {
-                const unsigned long long g = gb + k;
-                if (g < p.out_cap) p.out[g] = s.out[k];
-                else atomicOr(&p.ctr->err, kErrOutOvf);
-            }
+            store_run(p, s.gbase, s.out, nv, t, kPairThreads);
             __syncthreads();
             if (t == 0) {
                 s.out_n = 0;
@@ -1752,7 +1813,21 @@ cudaError_t launch_expand(const Params& p, cudaStream_t st) {
 }
 
 template <int D, bool B, bool N, bool R = false>
-static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st, cudaEvent_t* ev, unsigned evf) {
+static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st, cudaEvent_t* ev, unsigned evf,
+                                  const PairOverlap* ov) {
+    if (ov && !R && ov->side_sms > 0 && ov->side_sms < sm_count) {
+        cudaError_t e;
+        if ((e = cudaEventRecord(ov->fork, st)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(ov->side, ov->fork, 0)) != cudaSuccess) return e;
+        k_pairs_small<D, B, N, R><<<ov->side_sms * g_blocks_small, kPairThreads, 0, ov->side>>>(p);
+        if (ev) cudaEventRecordWithFlags(ev[0], ov->side, evf);
+        k_pairs_block<D, B, N, R><<<ov->side_sms * g_blocks_block, kPairThreads, sizeof(BlockSmem), ov->side>>>(p);
+        k_pairs_med<D, B, N, R><<<(sm_count - ov->side_sms) * g_blocks_med, kPairThreads, med_smem(), st>>>(p);
+        if (ev) cudaEventRecordWithFlags(ev[1], st, evf);
+        if ((e = cudaEventRecord(ov->join, ov->side)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(st, ov->join, 0)) != cudaSuccess) return e;
+        return cudaGetLastError();
+    }
     k_pairs_small<D, B, N, R><<<sm_count * g_blocks_small, kPairThreads, 0, st>>>(p);
     if (ev) cudaEventRecordWithFlags(ev[0], st, evf);
     k_pairs_med<D, B, N, R><<<sm_count * g_blocks_med, kPairThreads, med_smem(), st>>>(p);
@@ -1762,22 +1837,23 @@ static cudaError_t launch_pairs_t(const Params& p, int sm_count, cudaStream_t st
     return cudaGetLastError();
 }
 
-cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev, unsigned evf) {
+cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev, unsigned evf,
+                         const PairOverlap* ov) {
     const bool bip = p.split != kNoSplit;
     const bool narrow = p.max_range <= (1u << kMissShift);
     if (p.records) {  // record mode: self queries
         if (bip) return cudaErrorInvalidValue;
-        if (narrow) return dims == 2 ? launch_pairs_t<2, false, true, true>(p, sm_count, st, ev, evf)
-                                     : launch_pairs_t<3, false, true, true>(p, sm_count, st, ev, evf);
-        return dims == 2 ? launch_pairs_t<2, false, false, true>(p, sm_count, st, ev, evf)
-                         : launch_pairs_t<3, false, false, true>(p, sm_count, st, ev, evf);
+        if (narrow) return dims == 2 ? launch_pairs_t<2, false, true, true>(p, sm_count, st, ev, evf, ov)
+                                     : launch_pairs_t<3, false, true, true>(p, sm_count, st, ev, evf, ov);
+        return dims == 2 ? launch_pairs_t<2, false, false, true>(p, sm_count, st, ev, evf, ov)
+                         : launch_pairs_t<3, false, false, true>(p, sm_count, st, ev, evf, ov);
     }
     if (narrow) {
-        if (dims == 2) return bip ? launch_pairs_t<2, true, true>(p, sm_count, st, ev, evf) : launch_pairs_t<2, false, true>(p, sm_count, st, ev, evf);
-        return bip ? launch_pairs_t<3, true, true>(p, sm_count, st, ev, evf) : launch_pairs_t<3, false, true>(p, sm_count, st, ev, evf);
+        if (dims == 2) return bip ? launch_pairs_t<2, true, true>(p, sm_count, st, ev, evf, ov) : launch_pairs_t<2, false, true>(p, sm_count, st, ev, evf, ov);
+        return bip ? launch_pairs_t<3, true, true>(p, sm_count, st, ev, evf, ov) : launch_pairs_t<3, false, true>(p, sm_count, st, ev, evf, ov);
     }
-    if (dims == 2) return bip ? launch_pairs_t<2, true, false>(p, sm_count, st, ev, evf) : launch_pairs_t<2, false, false>(p, sm_count, st, ev, evf);
-    return bip ? launch_pairs_t<3, true, false>(p, sm_count, st, ev, evf) : launch_pairs_t<3, false, false>(p, sm_count, st, ev, evf);
+    if (dims == 2) return bip ? launch_pairs_t<2, true, false>(p, sm_count, st, ev, evf, ov) : launch_pairs_t<2, false, false>(p, sm_count, st, ev, evf, ov);
+    return bip ? launch_pairs_t<3, true, false>(p, sm_count, st, ev, evf, ov) : launch_pairs_t<3, false, false>(p, sm_count, st, ev, evf, ov);
 }
 
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,

@@ -94,6 +94,14 @@ struct Params {
     const uint32_t* merged;       // merged mode (one scene): cell -> root of its merged block, or kUnmerged
     uint32_t records;             // record mode: work lists hold {cell id, n}; the pair kernels write the
                                   // reference's Rice record stream (8-byte words) instead of pairs
+    // upload fused into the count: when box_copy is set, the count reads the
+    // boxes from page-locked host memory (boxes [0, up_split) at up_red, the
+    // rest at up_blue, device-mapped addresses) and writes them to box_copy,
+    // the device copy (== boxes) that the later kernels read
+    const uint32_t* up_red;
+    const uint32_t* up_blue;
+    uint64_t up_split;
+    uint32_t* box_copy;
 };
 
 constexpr uint32_t kUnmerged = 0x0fffff11u;  // a cell outside every merged block
@@ -108,10 +116,22 @@ cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st);
 // exclusive scan of nscenes+1 per-scene pair counts (one block)
 cudaError_t launch_scene_offsets(const Params& p, const unsigned long long* hist, unsigned long long* off,
                                  uint32_t nscenes_cap, cudaStream_t st);
+// Pairs bound for page-locked host memory are limited by the host link, not
+// by the kernels: with an overlap the small-cell and block kernels run on
+// `side` over side_sms SMs while the medium-cell kernel runs on the others,
+// so the link stays busy while the lighter kernels compute. `fork` and
+// `join` are events owned by the caller.
+struct PairOverlap {
+    cudaStream_t side;
+    cudaEvent_t fork, join;
+    int side_sms;
+};
+
 // ev (optional, 2 events) is recorded after the small-cell and after the
-// medium-cell kernel
+// medium-cell kernel (with an overlap: after the small-cell kernel on the side
+// stream and after the medium-cell kernel on st)
 cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t st, cudaEvent_t* ev = nullptr,
-                         unsigned ev_flags = cudaEventRecordDefault);
+                         unsigned ev_flags = cudaEventRecordDefault, const PairOverlap* ov = nullptr);
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,
                                   unsigned long long* scene_cursor, uint2* dst, cudaStream_t st);
 cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st);

@@ -291,6 +291,12 @@ class Engine:
                                           vp(recs.ctypes.data)))
         return words, start_i, recs
 
+    def set_host_split(self, sms: int) -> None:
+        """SMs of the small-cell and block kernels beside the medium-cell
+        kernel when pairs go to page-locked host memory (0: automatic, a
+        quarter; negative: one after another)."""
+        _check(self._L.pbig2_set_option(self._ctx, 4, int(sms)))
+
     def set_graphs(self, on: bool) -> None:
         """Capture/replay batched queries as CUDA graphs (on by default)."""
         _check(self._L.pbig2_set_option(self._ctx, 1, int(bool(on))))

@@ -186,6 +186,69 @@ def test_direct_pair_output(engine):
     assert engine.self_intersect(boxes, gen.RANGE) == n and not engine.result_in(out)
 
 
+@pytest.mark.parametrize("split", [-1, 0, 8, 100])
+def test_host_output_split(engine, split):
+    """Pairs to page-locked host memory with the small-cell and block kernels
+    beside the medium-cell kernel (any SM share) or after it: the same pair
+    set, self and red/blue, with cells of every class (a stack of identical
+    boxes fills the block kernel)."""
+    import torch
+    boxes = gen.clustered3d(200000, seed=9)
+    stack = np.repeat(boxes[:1], 3000, axis=0)
+    boxes = np.concatenate([boxes, stack])
+    boxes[:, 6] = np.arange(boxes.shape[0])
+    n = engine.self_intersect(boxes, gen.RANGE)
+    want = canon(engine.pairs())
+    red, blue = gen.mixed3d(100000, seed=0), gen.mixed3d(100000, seed=1)
+    nb = engine.bipartite_intersect(red, blue, gen.RANGE)
+    want_b = canon(engine.pairs())
+    out = torch.empty((max(n, nb) + 64, 2), dtype=torch.int32).pin_memory()
+    try:
+        engine.set_host_split(split)
+        engine.set_pair_output(out)
+        assert engine.self_intersect(boxes, gen.RANGE) == n and engine.result_in(out)
+        assert np.array_equal(canon(out[:n].numpy().view(np.uint32)), want)
+        assert engine.bipartite_intersect(red, blue, gen.RANGE) == nb and engine.result_in(out)
+        assert np.array_equal(canon(out[:nb].numpy().view(np.uint32)), want_b)
+        with pytest.raises(PbigError):
+            engine.set_host_split(100000)
+    finally:
+        engine.set_pair_output(None)
+        engine.set_host_split(0)
+
+
+@pytest.mark.parametrize("dims", [2, 3])
+def test_pinned_host_input(engine, dims):
+    """Page-locked host input is uploaded by the count kernel itself (no copy
+    before the pipeline): the same pairs as pageable input for self and
+    red/blue queries of ragged sizes (a count tile straddles red and blue),
+    with one side pinned and the other pageable, and in merged mode."""
+    import torch
+
+    def pin(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).pin_memory()
+
+    boxes = gen.clustered3d(100003, seed=3) if dims == 3 else gen.uniform2d(100003, seed=3)
+    n = engine.self_intersect(boxes, gen.RANGE)
+    want = canon(engine.pairs())
+    assert engine.self_intersect(pin(boxes), gen.RANGE) == n
+    assert np.array_equal(canon(engine.pairs()), want)
+    red, blue = boxes[:50001].copy(), boxes[50001:].copy()
+    blue[:, -1] = np.arange(blue.shape[0])
+    nb = engine.bipartite_intersect(red, blue, gen.RANGE)
+    want_b = canon(engine.pairs())
+    assert engine.bipartite_intersect(pin(red), pin(blue), gen.RANGE) == nb
+    assert np.array_equal(canon(engine.pairs()), want_b)
+    assert engine.bipartite_intersect(pin(red), blue, gen.RANGE) == nb
+    assert np.array_equal(canon(engine.pairs()), want_b)
+    engine.set_merged(True)
+    try:
+        assert engine.self_intersect(pin(boxes), gen.RANGE) == n
+        assert np.array_equal(canon(engine.pairs()), want)
+    finally:
+        engine.set_merged(False)
+
+
 def test_output_capacity_growth(engine):
     """A tiny scene first (small buffers), then one with millions of pairs:
     the pair buffer must grow and the count stay exact."""
