@@ -89,9 +89,16 @@ uint32_t nrc_for(uint32_t range, uint32_t shift) {
 // (C cells, E box-in-cell entries, T pair tests), estimated from a sample.
 // T is counted exactly on the sample (cell occupancy by hashing) and scaled
 // by (n/m)^2, since a pair of boxes survives sampling with probability
-// (m/n)^2.
+// (m/n)^2. A test costs more once the tests sit in cells beyond the
+// medium-cell kernel's reach: with the entry-weighted mean occupancy
+// m = 2T/E + 1, kTest is scaled by max(1, m / kOccTest). The constants are
+// fitted on GB300 cell-size sweeps (2-D/3-D, uniform/clustered, single
+// scenes and a 4096-scene batch), where they pick the fastest size or one
+// within 2%; per unit, an entry costs ~16 ps in the count and scatter plus
+// its fetch and sweep in the pair kernels, a test ~1 ps in the medium-cell
+// kernel and ~2 ps in the block kernel.
 // --------------------------------------------------------------------------
-static const double kCell = 1.2e-12, kEntry = 4.0e-12, kTest = 0.45e-12;
+static const double kCell = 2.4e-12, kEntry = 80.0e-12, kTest = 0.9e-12, kOccTest = 96.0;
 
 // pair tests of the sample at one cell size: occupancy of the sample's cells
 // counted in an open-addressing hash table (key = cell id + 1)
@@ -179,7 +186,8 @@ static TuneResult tune_impl(const uint32_t* boxes, const std::vector<uint64_t>& 
         } else {
             T = E * E / (2.0 * C);
         }
-        const double cost = kCell * C + kEntry * E + kTest * T;
+        const double occ = 2.0 * T / std::max(E, 1.0) + 1.0;
+        const double cost = kCell * C + kEntry * E + kTest * std::max(1.0, occ / kOccTest) * T;
         if (cost < best_cost) {
             best_cost = cost;
             best = TuneResult{(uint32_t)s, E, T, C};
