@@ -391,6 +391,7 @@ def run_gb300(args, rank, local, ws):
                 "frac_of_" + peak_kind: (algo[k] / (phase[k] * 1e-3) / 1e9) / peak if phase[k] > 0 else None}
             for k in algo}
     kern["pairs"]["pair_tests_per_s"] = stats["pair_tests"] / (phase["pairs"] * 1e-3)
+    kern["pairs"]["split_ms"] = {k: phase.get("pairs_" + k, 0.0) for k in ("small", "med", "block")}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_step * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -126,6 +126,16 @@ __device__ __forceinline__ void stage_upload(const Params& p, uint64_t b0, uint3
     }
 }
 
+// n / d (d >= 1) by a multiply-high with the divisor's multiplier m =
+// magic_of(d) = ceil(2^32 / d) (0 for d = 1): for n < 2^31 the estimate is
+// exact or one too large, which one compare fixes
+__device__ __forceinline__ uint32_t magic_of(uint32_t d) { return d > 1u ? 0xffffffffu / d + 1u : 0u; }
+__device__ __forceinline__ uint32_t div_magic(uint32_t n, uint32_t d, uint32_t m) {
+    if (m == 0u) return n;
+    const uint32_t q = __umulhi(n, m);
+    return q * d > n ? q - 1u : q;
+}
+
 template <int D, bool SCATTER, bool MERGED>
 __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t* sbox, uint64_t b0,
                                                 uint32_t nb) {
@@ -169,6 +179,7 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
     const uint32_t total = __shfl_sync(FULL_MASK, incl, 31);
     const uint32_t excl = incl - cnt;
     const uint64_t wbox0 = b0 + (t & ~31u);
+    const uint32_t mx = magic_of(sx), my = magic_of(sy);  // one division per box, none per cell
     for (uint32_t q0 = 0; q0 < total; q0 += 32) {
         const uint32_t q = q0 + lane;
         uint32_t o = 0;  // owner lane: number of lanes whose inclusive count <= q
@@ -182,10 +193,12 @@ __device__ __forceinline__ void enumerate_cells(const Params& p, const uint32_t*
         const uint32_t o_sy = __shfl_sync(FULL_MASK, sy, o);
         const uint32_t o_nrc = __shfl_sync(FULL_MASK, nrc, o);
         const uint64_t o_base = __shfl_sync(FULL_MASK, base, o);
+        const uint32_t o_mx = __shfl_sync(FULL_MASK, mx, o);
+        const uint32_t o_my = __shfl_sync(FULL_MASK, my, o);
         if (q < total) {
-            const uint32_t lq = q - o_excl;
-            const uint32_t i = lq % o_sx, rr = lq / o_sx;
-            const uint32_t j = rr % o_sy, k = rr / o_sy;
+            const uint32_t lq = q - o_excl;  // < 2^26
+            const uint32_t rr = div_magic(lq, o_sx, o_mx), i = lq - rr * o_sx;
+            const uint32_t k = div_magic(rr, o_sy, o_my), j = rr - k * o_sy;
             uint64_t gid = o_base + ((uint64_t)k * o_nrc + j) * o_nrc + i;
             uint32_t f = (i == 0 ? 1u : 0u) | (j == 0 ? 2u : 0u) | ((D == 2 || k == 0) ? 4u : 0u);
             bool take = true;
@@ -261,7 +274,7 @@ __global__ void __launch_bounds__(kBoxThreads) k_scatter(Params pin) {
 
 // ---------------------------------------------------------------------------
 // scan: counts -> cell starts and the work lists of the pair kernels, in
-// three launches without inter-block waits.
+// two launches without inter-block waits.
 //
 // A tile is 4096 cells, a chunk 512 of them; every warp works on whole
 // chunks with no block barrier, so the loads of all resident warps are in
@@ -271,9 +284,10 @@ __global__ void __launch_bounds__(kBoxThreads) k_scatter(Params pin) {
 //   k_scan_reduce  chunk entry total (stored per chunk, added to the tile)
 //                  and the pair tests of its cells (added to the tile);
 //                  two chunks per warp iteration, so eight 16-byte loads
-//                  per lane are in flight together.
-//   k_scan_prefix  one block: tile entry totals -> exclusive prefixes; the
-//                  entry and pair-test totals go to the counters.
+//                  per lane are in flight together. The last block to
+//                  finish turns the tile entry totals into exclusive
+//                  prefixes; the entry and pair-test totals go to the
+//                  counters.
 //   k_scan_cells   the same chunks again: starts from the tile prefix, the
 //                  tile's earlier chunks and a warp scan; every cell of two
 //                  or more boxes goes to its work list, a chunk reserving
@@ -292,7 +306,7 @@ constexpr int kScanChunks = 8;                               // chunks per tile
 constexpr int kScanTile = kScanChunk * kScanChunks;
 
 struct TileRec {                         // 64 bytes per tile
-    unsigned long long sum;              // entries; exclusive prefix after k_scan_prefix
+    unsigned long long sum;              // entries; exclusive prefix after k_scan_reduce
     unsigned long long tests;            // pair tests of the tile's cells
     uint32_t chunk[kScanChunks];         // entries per chunk
     unsigned long long comp;             // sum of n*n/2 over the tile's cells of n >= 2
@@ -376,44 +390,30 @@ __device__ __forceinline__ void reduce_chunk(TileRec* rec, uint64_t ch, const ui
     }
 }
 
-__global__ void __launch_bounds__(kScanThreads, 4) k_scan_reduce(Params pin) {
-    const Params p = resolve(pin);
-    const uint32_t warp = threadIdx.x >> 5;
-    const uint64_t chunks = (p.ncells + kScanChunk - 1) / kScanChunk;
-    TileRec* rec = reinterpret_cast<TileRec*>(p.tile_state);
-    const uint64_t nw = (uint64_t)gridDim.x * (kScanThreads / 32);
-    for (uint64_t ch = 2 * ((uint64_t)blockIdx.x * (kScanThreads / 32) + warp); ch < chunks; ch += 2 * nw) {
-        uint32_t v[kScanPerThread], w[kScanPerThread];
-        scan_load(p, ch, v);
-        const bool two = ch + 1 < chunks;
-        if (two) scan_load(p, ch + 1, w);
-        reduce_chunk(rec, ch, v);
-        if (two) reduce_chunk(rec, ch + 1, w);
-    }
-}
-
-constexpr int kPrefixThreads = 1024;
-__global__ void __launch_bounds__(kPrefixThreads) k_scan_prefix(Params pin) {
-    __shared__ unsigned long long s_part[kPrefixThreads / 32][4];
+// tile entry totals -> exclusive prefixes; the entry, pair-test and job
+// totals go to the counters. Run by one block of kReduceThreads threads.
+constexpr int kReduceThreads = 1024;
+__device__ __forceinline__ void scan_prefix_block(const Params& p) {
+    __shared__ unsigned long long s_part[kReduceThreads / 32][4];
     __shared__ unsigned long long s_carry[4];
-    const Params p = resolve(pin);
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const uint64_t tiles = (p.ncells + kScanTile - 1) / kScanTile;
     TileRec* rec = reinterpret_cast<TileRec*>(p.tile_state);
     if (t == 0) s_carry[0] = s_carry[1] = s_carry[2] = s_carry[3] = 0;
-    // rounds of 4 tiles per thread: all loads of a round in flight together
-    for (uint64_t r0 = 0; r0 < tiles; r0 += 4 * kPrefixThreads) {
+    // rounds of 4 tiles per thread: all loads of a round in flight together;
+    // the records were written through L2 by other blocks (read past L1)
+    for (uint64_t r0 = 0; r0 < tiles; r0 += 4 * kReduceThreads) {
         unsigned long long x[4], sx = 0, sy = 0, sc = 0, sj = 0, sm = 0;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const uint64_t i = r0 + 4 * (uint64_t)t + k;
-            x[k] = i < tiles ? rec[i].sum : 0ull;
+            x[k] = i < tiles ? __ldcg(&rec[i].sum) : 0ull;
             sx += x[k];
             if (i < tiles) {
-                sy += rec[i].tests;
-                sc += rec[i].comp;
-                sj += rec[i].jobs;
-                sm = max(sm, (unsigned long long)rec[i].maxc);
+                sy += __ldcg(&rec[i].tests);
+                sc += __ldcg(&rec[i].comp);
+                sj += __ldcg(&rec[i].jobs);
+                sm = max(sm, (unsigned long long)__ldcg(&rec[i].maxc));
             }
         }
         const unsigned long long ix = warp_incl_scan64(sx);
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(kPrefixThreads) k_scan_prefix(Params pin) {
         }
         __syncthreads();
         unsigned long long wo = s_carry[0], tot = 0, tt = 0, tc = 0, tj = 0, tm = 0;
-        for (int w = 0; w < kPrefixThreads / 32; w++) {
+        for (int w = 0; w < kReduceThreads / 32; w++) {
             const unsigned long long a = s_part[w][0];
             if (w < (int)warp) wo += a;
             tot += a;
@@ -461,6 +461,33 @@ __global__ void __launch_bounds__(kPrefixThreads) k_scan_prefix(Params pin) {
         p.ctr->max_cell = (uint32_t)(s_carry[3] & 0xffffffffull);
         if (total >= (1ull << 32)) atomicOr(&p.ctr->err, kErrEntryOvf);
     }
+}
+
+// one block per SM; the last block to finish (a ticket taken after a fence,
+// no waiting) runs the tile prefix, so no separate launch is needed for it
+__global__ void __launch_bounds__(kReduceThreads, 1) k_scan_reduce(Params pin) {
+    __shared__ uint32_t s_last;
+    const Params p = resolve(pin);
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint64_t chunks = (p.ncells + kScanChunk - 1) / kScanChunk;
+    TileRec* rec = reinterpret_cast<TileRec*>(p.tile_state);
+    const uint64_t nw = (uint64_t)gridDim.x * (kReduceThreads / 32);
+    for (uint64_t ch = 2 * ((uint64_t)blockIdx.x * (kReduceThreads / 32) + warp); ch < chunks; ch += 2 * nw) {
+        uint32_t v[kScanPerThread], w[kScanPerThread];
+        scan_load(p, ch, v);
+        const bool two = ch + 1 < chunks;
+        if (two) scan_load(p, ch + 1, w);
+        reduce_chunk(rec, ch, v);
+        if (two) reduce_chunk(rec, ch + 1, w);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&p.ctr->ticket, 1u) == gridDim.x - 1 ? 1u : 0u;
+    __syncthreads();
+    if (s_last == 0u) return;
+    __threadfence();
+    scan_prefix_block(p);
+    if (threadIdx.x == 0) p.ctr->ticket = 0;  // the next scan needs no reset
 }
 
 // ---- bulk asynchronous copies (global -> shared) completing on an mbarrier
@@ -1110,7 +1137,7 @@ __device__ __forceinline__ void rec_hits(const Params& p, const WarpOut& o) {
 }
 
 template <int D, bool BIP, bool NARROW, bool REC = false>
-__global__ void __launch_bounds__(kPairThreads, 6) k_pairs_small(Params p) {
+__global__ void __launch_bounds__(kPairThreads, 5) k_pairs_small(Params p) {
     __shared__ uint4 s_a[kPairWarps][kSmallSlots], s_b[kPairWarps][kSmallSlots];
     __shared__ uint2 s_out[kPairWarps][kWarpOut];
     const uint32_t warp = threadIdx.x >> 5;
@@ -1787,13 +1814,15 @@ cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st) {
 cudaError_t launch_scan(const Params& p, cudaStream_t st) {
     const uint64_t chunks = (p.ncells + kScanChunk - 1) / kScanChunk;
     const uint64_t blocks = (chunks + kScanThreads / 32 - 1) / (kScanThreads / 32);
-    const uint64_t cap = (uint64_t)(g_sm_count > 0 ? g_sm_count : 152) * 4;  // resident: 4 blocks per SM
+    const uint64_t sms = (uint64_t)(g_sm_count > 0 ? g_sm_count : 152);
+    const uint64_t cap = sms * 4;  // resident: 4 blocks per SM
     const unsigned g = (unsigned)(blocks < cap ? (blocks ? blocks : 1) : cap);
-    const unsigned g2 = (unsigned)((blocks + 1) / 2 < cap ? ((blocks + 1) / 2 ? (blocks + 1) / 2 : 1) : cap);
+    // reduce: one 1024-thread block per SM, two chunks per warp item
+    const uint64_t rblocks = (chunks + 2 * (kReduceThreads / 32) - 1) / (2 * (kReduceThreads / 32));
+    const unsigned g2 = (unsigned)(rblocks < sms ? (rblocks ? rblocks : 1) : sms);
     cudaError_t e = cudaMemsetAsync(p.tile_state, 0, scan_state_bytes(p.ncells), st);
     if (e != cudaSuccess) return e;
-    k_scan_reduce<<<g2, kScanThreads, 0, st>>>(p);
-    k_scan_prefix<<<1, kPrefixThreads, 0, st>>>(p);
+    k_scan_reduce<<<g2, kReduceThreads, 0, st>>>(p);
     k_scan_cells<<<g, kScanThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
