@@ -391,8 +391,10 @@ __device__ __forceinline__ void reduce_chunk(TileRec* rec, uint64_t ch, const ui
 }
 
 // tile entry totals -> exclusive prefixes; the entry, pair-test and job
-// totals go to the counters. Run by one block of kReduceThreads threads.
-constexpr int kReduceThreads = 1024;
+// totals go to the counters. Run by one block of kReduceThreads threads,
+// kPrefixPer tiles per thread per round (4096 tiles in two rounds).
+constexpr int kReduceThreads = kScanThreads;
+constexpr int kPrefixPer = 8;
 __device__ __forceinline__ void scan_prefix_block(const Params& p) {
     __shared__ unsigned long long s_part[kReduceThreads / 32][4];
     __shared__ unsigned long long s_carry[4];
@@ -400,13 +402,14 @@ __device__ __forceinline__ void scan_prefix_block(const Params& p) {
     const uint64_t tiles = (p.ncells + kScanTile - 1) / kScanTile;
     TileRec* rec = reinterpret_cast<TileRec*>(p.tile_state);
     if (t == 0) s_carry[0] = s_carry[1] = s_carry[2] = s_carry[3] = 0;
-    // rounds of 4 tiles per thread: all loads of a round in flight together;
-    // the records were written through L2 by other blocks (read past L1)
-    for (uint64_t r0 = 0; r0 < tiles; r0 += 4 * kReduceThreads) {
-        unsigned long long x[4], sx = 0, sy = 0, sc = 0, sj = 0, sm = 0;
+    // rounds of kPrefixPer tiles per thread: all loads of a round in flight
+    // together; the records were written through L2 by other blocks (read
+    // past L1)
+    for (uint64_t r0 = 0; r0 < tiles; r0 += kPrefixPer * kReduceThreads) {
+        unsigned long long x[kPrefixPer], sx = 0, sy = 0, sc = 0, sj = 0, sm = 0;
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const uint64_t i = r0 + 4 * (uint64_t)t + k;
+        for (int k = 0; k < kPrefixPer; k++) {
+            const uint64_t i = r0 + kPrefixPer * (uint64_t)t + k;
             x[k] = i < tiles ? __ldcg(&rec[i].sum) : 0ull;
             sx += x[k];
             if (i < tiles) {
@@ -438,8 +441,8 @@ __device__ __forceinline__ void scan_prefix_block(const Params& p) {
         }
         unsigned long long run = wo + (ix - sx);
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const uint64_t i = r0 + 4 * (uint64_t)t + k;
+        for (int k = 0; k < kPrefixPer; k++) {
+            const uint64_t i = r0 + kPrefixPer * (uint64_t)t + k;
             if (i < tiles) rec[i].sum = run;
             run += x[k];
         }
@@ -463,9 +466,9 @@ __device__ __forceinline__ void scan_prefix_block(const Params& p) {
     }
 }
 
-// one block per SM; the last block to finish (a ticket taken after a fence,
-// no waiting) runs the tile prefix, so no separate launch is needed for it
-__global__ void __launch_bounds__(kReduceThreads, 1) k_scan_reduce(Params pin) {
+// the last block to finish (a ticket taken after a fence, no waiting) runs
+// the tile prefix, so no separate launch is needed for it
+__global__ void __launch_bounds__(kReduceThreads, 4) k_scan_reduce(Params pin) {
     __shared__ uint32_t s_last;
     const Params p = resolve(pin);
     const uint32_t warp = threadIdx.x >> 5;
@@ -1817,9 +1820,9 @@ cudaError_t launch_scan(const Params& p, cudaStream_t st) {
     const uint64_t sms = (uint64_t)(g_sm_count > 0 ? g_sm_count : 152);
     const uint64_t cap = sms * 4;  // resident: 4 blocks per SM
     const unsigned g = (unsigned)(blocks < cap ? (blocks ? blocks : 1) : cap);
-    // reduce: one 1024-thread block per SM, two chunks per warp item
+    // reduce: two chunks per warp item, 4 resident blocks per SM
     const uint64_t rblocks = (chunks + 2 * (kReduceThreads / 32) - 1) / (2 * (kReduceThreads / 32));
-    const unsigned g2 = (unsigned)(rblocks < sms ? (rblocks ? rblocks : 1) : sms);
+    const unsigned g2 = (unsigned)(rblocks < cap ? (rblocks ? rblocks : 1) : cap);
     cudaError_t e = cudaMemsetAsync(p.tile_state, 0, scan_state_bytes(p.ncells), st);
     if (e != cudaSuccess) return e;
     k_scan_reduce<<<g2, kReduceThreads, 0, st>>>(p);
