@@ -282,6 +282,7 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
     }
     if (full) {
         R(cudaMemsetAsync(p.ctr, 0, sizeof(Ctr), st));
+        if (p.scene_table) R(launch_scene_table(p, st));
         R(cudaEventRecordWithFlags(c->evp[0], st, evf));
         R(launch_count(p, dims, st));
         R(cudaEventRecordWithFlags(c->evp[1], st, evf));
@@ -412,7 +413,7 @@ static int capture_graph(pbig2_ctx* c, const Params& p0, const uint32_t* d_boxes
     G.nscenes_cap = nsc;
     G.entry_cap = p.entry_cap;
     G.out_cap = p.out_cap;
-    G.launches = 12;  // count, scan (3), expand, scatter, pairs (3), scene grouping (3)
+    G.launches = 13;  // scene table, count (2), scan (2), expand, scatter, pairs (3), scene grouping (3)
     G.buffers = c->buffers_sig();
     return PBIG2_OK;
 }
@@ -594,6 +595,10 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     }
     p.scenes = c->d_scenes.as<Scene>();
     p.scene_box_off = c->d_scene_off.as<uint32_t>();
+    if (grouped) {  // many scenes: the scene of every 256th box, for the scene lookups of the kernels
+        CK(c->d_scene_tab.ensure(scene_table_entries(nboxes) * 4, false, st));
+        p.scene_table = c->d_scene_tab.as<uint32_t>();
+    }
     p.nscenes = nsc;
     p.split = split;
     p.max_range = range;
@@ -641,7 +646,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
                 return fail(PBIG2_ECUDA, "pipeline launch (engine.cu:%d): %s", g_record_line, cudaGetErrorString(re));
         }
         launches += need_full ? 6 : 0;  // count, scan (3), expand, scatter
-        launches += 3 + (grouped ? 3 : 0) + (p.records ? 1 : 0);
+        launches += 3 + (grouped ? 3 : 0) + (p.records ? 1 : 0) + (need_full && p.scene_table ? 1 : 0);
         CK(cudaMemcpyAsync(c->h_ctr.p, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, st));
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
@@ -776,7 +781,7 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_entries,
                       &c->d_lists, &c->d_tasks, &c->d_state,
                       &c->d_out, &c->d_out2, &c->d_ctr, &c->d_scenes, &c->d_scene_off, &c->d_scene_pair,
-                      &c->d_scene_cursor, &c->d_dims})
+                      &c->d_scene_cursor, &c->d_dims, &c->d_scene_tab})
         b->release();
     c->h_ctr.release();
     c->h_stage.release();

@@ -61,7 +61,7 @@ struct pbig2_ctx {
     uint64_t last_ncells = 0, last_entries = 0;
     uint32_t merged_blocks = 0;  // merged blocks of the last query
     pbig::DevBuf d_boxes, d_counts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
-        d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims;
+        d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims, d_scene_tab;
     pbig::HostPinned h_ctr, h_stage;
     // caller's pair buffer for self/bipartite queries (pbig2_set_pair_output)
     uint2* ext_out = nullptr;
@@ -99,7 +99,8 @@ struct pbig2_ctx {
     uintptr_t buffers_sig() const {
         uintptr_t h = 0;
         for (const pbig::DevBuf* b : {&d_counts, &d_entries, &d_lists, &d_tasks, &d_state, &d_out, &d_out2,
-                                      &d_ctr, &d_scenes, &d_scene_off, &d_scene_pair, &d_scene_cursor, &d_dims})
+                                      &d_ctr, &d_scenes, &d_scene_off, &d_scene_pair, &d_scene_cursor, &d_dims,
+                                      &d_scene_tab})
             h = h * 1000003u + (uintptr_t)b->p;
         return h * 1000003u + (uintptr_t)h_ctr.p;
     }

@@ -56,15 +56,35 @@ __device__ __forceinline__ Params resolve(const Params& in) {
     return p;
 }
 
-__device__ __forceinline__ uint32_t find_scene(const Params& p, uint64_t gi) {
-    if (p.nscenes <= 1) return 0;
-    uint32_t lo = 0, hi = p.nscenes;  // last scene s with scene_box_off[s] <= gi
+// the last scene s in [lo, hi) with scene_box_off[s] <= gi
+__device__ __forceinline__ uint32_t search_scene(const Params& p, uint64_t gi, uint32_t lo, uint32_t hi) {
     while (hi - lo > 1) {
         uint32_t mid = (lo + hi) >> 1;
         if (p.scene_box_off[mid] <= gi) lo = mid;
         else hi = mid;
     }
     return lo;
+}
+
+// scene of global box gi: with the scene table (scene of every 256th box)
+// the search covers only the scenes that start inside gi's 256-box block
+constexpr uint32_t kSceneTableShift = 8;
+__device__ __forceinline__ uint32_t find_scene(const Params& p, uint64_t gi) {
+    if (p.nscenes <= 1) return 0;
+    if (p.scene_table) {
+        const uint64_t b = gi >> kSceneTableShift;
+        const uint32_t s0 = p.scene_table[b];
+        const uint32_t s1 = ((b + 1) << kSceneTableShift) < p.nboxes ? p.scene_table[b + 1] : p.nscenes - 1;
+        return search_scene(p, gi, s0, s1 + 1);
+    }
+    return search_scene(p, gi, 0, p.nscenes);
+}
+
+__global__ void k_scene_table(Params pin) {
+    const Params p = resolve(pin);
+    const uint64_t n = (p.nboxes + (1u << kSceneTableShift) - 1) >> kSceneTableShift;
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < n; b += (uint64_t)gridDim.x * blockDim.x)
+        p.scene_table[b] = p.nscenes <= 1 ? 0u : search_scene(p, b << kSceneTableShift, 0, p.nscenes);
 }
 
 // ---------------------------------------------------------------------------
@@ -1780,6 +1800,16 @@ cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStr
 }
 
 uint64_t scan_tiles(uint64_t ncells) { return (ncells + kScanTile - 1) / kScanTile; }
+
+uint64_t scene_table_entries(uint64_t nboxes) { return (nboxes >> kSceneTableShift) + 2; }
+
+cudaError_t launch_scene_table(const Params& p, cudaStream_t st) {
+    const uint64_t n = scene_table_entries(p.nboxes);
+    const uint64_t cap = (uint64_t)(g_sm_count > 0 ? g_sm_count : 152) * 4;
+    const uint64_t g = (n + 255) / 256;
+    k_scene_table<<<(unsigned)(g < cap ? g : cap), 256, 0, st>>>(p);
+    return cudaGetLastError();
+}
 
 static unsigned box_grid(uint64_t nboxes) {
     const uint64_t nb = (nboxes + kBoxThreads - 1) / kBoxThreads;

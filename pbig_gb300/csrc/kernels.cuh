@@ -74,6 +74,7 @@ struct Params {
     uint64_t nboxes;              // boxes over all scenes
     const Scene* scenes;          // scene table (device)
     const uint32_t* scene_box_off;// nscenes+1 box offsets (device)
+    uint32_t* scene_table;        // batched queries: scene of box 256*b, per b (built by launch_scene_table)
     uint32_t nscenes;
     uint32_t split;               // bipartite: global index of the first blue box
     uint32_t max_range;           // largest scene range (selects the pair-test arithmetic)
@@ -135,6 +136,9 @@ cudaError_t launch_pairs(const Params& p, int dims, int sm_count, cudaStream_t s
 cudaError_t launch_group_by_scene(const Params& p, const unsigned long long* scene_pair_off,
                                   unsigned long long* scene_cursor, uint2* dst, cudaStream_t st);
 cudaError_t launch_scene_hist(const Params& p, unsigned long long* hist, cudaStream_t st);
+// p.scene_table for p.nboxes boxes (scene_table_entries of them)
+cudaError_t launch_scene_table(const Params& p, cudaStream_t st);
+uint64_t scene_table_entries(uint64_t nboxes);
 uint64_t scan_tiles(uint64_t ncells);
 size_t scan_state_bytes(uint64_t ncells);  // scan tile records
 size_t pair_smem_bytes();
