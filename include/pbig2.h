@@ -207,6 +207,36 @@ PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
 #define PBIG2_OPT_HOST_SPLIT 4
 PBIG2_API int pbig2_set_option(pbig2_ctx* ctx, int option, int64_t value);
 
+/* One batch of the serving loop (no counterpart in the reference; the
+ * request loop in pbig_gb300/serve.py decides the batches and where each
+ * scene lives). Runs, without returning to the caller in between: the cell
+ * size of every item whose shift is PBIG2_AUTO (tuned on a sample of its host
+ * rows; the choice is written back), the moved rows of updates (written into
+ * the item's host rows, and into its device rows unless the item is
+ * uploaded), uploads of items marked upload (host rows -> device rows), the
+ * concatenation of the items into cat_dev (cat_rows rows; not needed for one
+ * item), the batched query of the items as separate scenes, and the copy of
+ * the pairs (scene-local indices, grouped by item) into pairs_host (page-
+ * locked, pairs_cap pairs); scene_pair_off[n_items+1] gives each item's
+ * range. stage_host (page-locked) and stage_dev hold stage_rows staged update
+ * rows of 8 words. 3-D only. PBIG2_ECAPACITY: a buffer is too small (*npairs
+ * holds the pair count when the pair buffer was; the result stays on the
+ * device for pbig2_copy_pairs). */
+typedef struct {
+    uint32_t* dev;          /* the scene's rows on the device (n x 7 words) */
+    uint32_t* host;         /* the scene's rows on the host (n x 7 words) */
+    uint64_t n;             /* boxes of the scene */
+    const uint32_t* rows;   /* update: k new rows (7 words each), else null */
+    const uint32_t* idx;    /* update: their box indices */
+    uint64_t k;
+    uint32_t upload;        /* 1: copy the host rows to the device rows first */
+    uint32_t shift;         /* cell size; PBIG2_AUTO: tuned here, written back */
+} pbig2_batch_item;
+PBIG2_API int pbig2_serve_batch(pbig2_ctx* ctx, pbig2_batch_item* items, uint32_t n_items, uint32_t range,
+                                uint32_t* cat_dev, uint64_t cat_rows, uint32_t* stage_host, uint32_t* stage_dev,
+                                uint64_t stage_rows, void* stream, uint32_t* pairs_host, uint64_t pairs_cap,
+                                uint64_t* npairs, uint64_t* scene_pair_off, double* phase_ms);
+
 /* Allocation-free self-intersection (no counterpart in the reference).
  * For callers that cannot allocate device memory during the query -- a
  * process whose device memory is owned by another allocator, or a

@@ -27,7 +27,7 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("PBIG_NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 CUDA_HOME = os.path.dirname(os.path.dirname(os.path.realpath(NVCC)))
 
-ENGINE_SOURCES = ["engine.cu", "kernels.cu", "noalloc.cu", "update.cu"]
+ENGINE_SOURCES = ["engine.cu", "kernels.cu", "noalloc.cu", "update.cu", "serve_batch.cu"]
 ENGINE_HEADERS = ["kernels.cuh", "engine.h"]
 
 LIB_ENGINE = os.path.join(BUILD, "libpbig_gb300.so")

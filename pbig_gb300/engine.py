@@ -31,8 +31,14 @@ EXPORTS = [
     "pbig2_host_free", "pbig2_get_stats", "pbig2_tune_shift", "pbig2_self_intersect_noalloc",
     "pbig2_noalloc_last_error", "pbig2_set_option", "pbig2_scene_create", "pbig2_scene_destroy",
     "pbig2_scene_move", "pbig2_scene_delta", "pbig2_scene_pairs", "pbig2_scene_boxes", "pbig2_scene_copy",
-    "pbig2_result_records", "pbig2_copy_records", "pbig2_decode_records",
+    "pbig2_result_records", "pbig2_copy_records", "pbig2_decode_records", "pbig2_serve_batch",
 ]
+
+
+class BatchItem(C.Structure):
+    """pbig2_batch_item: one scene of a serving batch (pbig2_serve_batch)."""
+    _fields_ = [("dev", C.c_void_p), ("host", C.c_void_p), ("n", C.c_uint64), ("rows", C.c_void_p),
+                ("idx", C.c_void_p), ("k", C.c_uint64), ("upload", C.c_uint32), ("shift", C.c_uint32)]
 
 
 class PbigError(RuntimeError):
@@ -96,6 +102,8 @@ def lib():
         L.pbig2_self_intersect_noalloc.argtypes = [vp, u64, u32, u32, u32, vp, u64, C.POINTER(u64), vp]
         L.pbig2_noalloc_last_error.restype = C.c_char_p
         L.pbig2_set_option.argtypes = [vp, C.c_int, C.c_int64]
+        L.pbig2_serve_batch.argtypes = [vp, C.POINTER(BatchItem), u32, u32, vp, u64, vp, vp, u64, vp, vp, u64,
+                                        C.POINTER(u64), C.POINTER(u64), C.POINTER(C.c_double)]
         _LIB = L
     return _LIB
 
@@ -211,6 +219,24 @@ class Engine:
         self.last_rc = _check(rc)
         self._nscenes = ns
         return out.value
+
+    def serve_batch(self, items, range_: int, cat_dev: int, cat_rows: int, stage_host: int, stage_dev: int,
+                    stage_rows: int, stream, pairs_host: int, pairs_cap: int):
+        """One serving batch in native code (pbig2_serve_batch): items is a
+        ctypes array of BatchItem (cell sizes written back). Returns (rc,
+        pairs, per-item pair offsets, host phase ms); rc is OK or ECAPACITY
+        (a buffer too small: the pairs stay on the device)."""
+        ns = len(items)
+        npairs = C.c_uint64()
+        offs = np.zeros(ns + 1, dtype=np.uint64)
+        ph = (C.c_double * 4)()
+        rc = self._L.pbig2_serve_batch(self._ctx, items, ns, range_, C.c_void_p(cat_dev), cat_rows,
+                                       C.c_void_p(stage_host), C.c_void_p(stage_dev), stage_rows,
+                                       self._stream(stream), C.c_void_p(pairs_host), pairs_cap, C.byref(npairs),
+                                       offs.ctypes.data_as(C.POINTER(C.c_uint64)), ph)
+        self.last_rc = _check(rc, (OK, ECAPACITY))
+        self._nscenes = ns
+        return rc, npairs.value, offs, list(ph)
 
     def scene_offsets(self) -> np.ndarray:
         ns = self._nscenes

@@ -15,8 +15,10 @@ were on the GPU -- and resolves them as one batched query; two slots keep
 two batches in flight, so the copies and the host work of one overlap the
 kernels of the other. A scene is in at most one batch at a time.
 
-The engine calls release the GIL (ctypes), so the slot threads run
-concurrently.
+A batch's work after the admission decision -- cell sizes of new scenes,
+update rows, uploads, concatenation, the batched query and the download of
+the pairs -- is one native call (pbig2_serve_batch) that holds no
+interpreter lock, so the slot threads and the dispatcher run concurrently.
 """
 from __future__ import annotations
 
@@ -30,7 +32,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import gen
-from .engine import Engine, tune_shift
+from .engine import AUTO, ECAPACITY, BatchItem, Engine, tune_shift
 
 BOX_BYTES = 28
 WORK_BYTES_PER_BOX = 160  # device working memory of a query per box (grid, entries, lists, pairs)
@@ -158,7 +160,10 @@ class Server:
                 e.batch_intersect(boxes, offs, gen.RANGE, cell_shifts=shifts, stream=st)
                 e.sync(st)
             del boxes
+        # staged update rows (7 words and the box index), host and device
         self.staging = [torch.empty((1 << 16, 8), dtype=torch.int32).pin_memory() for _ in range(slots)]
+        self.stage_dev = [torch.empty((1 << 16, 8), dtype=torch.int32, device=f"cuda:{device}")
+                          for _ in range(slots)]
         self.free_slots = list(range(slots))
         self.batches = 0
         gc.collect()  # before the clock starts: serve() runs with the collector paused
@@ -202,12 +207,12 @@ class Server:
         self.resident_bytes -= sc.bytes
         self.evictions += 1
 
-    def _upload(self, sc: Scene, dev: str) -> None:
-        """Copy a scene to the device: into the arena (evicting idle scenes,
-        least recently used first, when it is too fragmented), else through
-        the caching allocator."""
+    def _place(self, sc: Scene, dev: str) -> None:
+        """Give a scene a device home (its rows are copied by the batch's
+        native step): in the arena (evicting idle scenes, least recently used
+        first, when it is too fragmented), else through the caching
+        allocator."""
         torch = self.torch
-        src = torch.from_numpy(sc.host.view(np.int32))
         with self.lock:
             off = self.arena.alloc(sc.host.size)
             while off is None:
@@ -218,11 +223,10 @@ class Server:
                 self._drop(victim)
                 off = self.arena.alloc(sc.host.size)
         if off is None:
-            sc.dev = src.to(dev, non_blocking=True)
+            sc.dev = torch.empty((sc.host.shape[0], 7), dtype=torch.int32, device=dev)
             return
         sc.arena_off = off
         sc.dev = self.arena.buf[off:off + sc.host.size].view(sc.host.shape[0], 7)
-        sc.dev.copy_(src, non_blocking=True)
 
     def _take_batch(self) -> list[Request]:
         """Pending requests that can run now (caller holds the lock)."""
@@ -269,6 +273,12 @@ class Server:
 
     # ---- batch execution (slot thread) ------------------------------------
     def _run_batch(self, slot: int, batch: list[Request]) -> None:
+        """A batch on one slot: device homes for scenes that need an upload
+        (Python, under the server lock), then one native call
+        (pbig2_serve_batch, no interpreter lock held) does the rest -- cell
+        sizes of new scenes, update rows into the host and device copies,
+        uploads, concatenation, the batched query and the download of the
+        pairs into the slot's page-locked buffer."""
         torch = self.torch
         eng = self.engines[slot]
         t_start = self.now()
@@ -278,47 +288,67 @@ class Server:
         dev = f"cuda:{self.device}"
         stream = self.streams[slot]
         tp = [time.perf_counter()]
-        with torch.cuda.stream(stream):
-            prep_split = self._prepare(batch, scenes, dev, slot)
-            tp.append(time.perf_counter())
-            offs = np.zeros(len(batch) + 1, dtype=np.uint64)
-            for i, sc in enumerate(scenes):
-                offs[i + 1] = offs[i] + sc.host.shape[0]
-            if len(scenes) == 1:
-                cat = scenes[0].dev
-            elif int(offs[-1]) <= self.catbuf[slot].shape[0]:
-                cat = torch.cat([sc.dev for sc in scenes], out=self.catbuf[slot][:int(offs[-1])])
-            else:
-                cat = torch.cat([sc.dev for sc in scenes])
-            shifts = np.array([sc.shift for sc in scenes], dtype=np.uint32)
-            tp.append(time.perf_counter())
-            total = eng.batch_intersect(cat, offs, gen.RANGE, cell_shifts=shifts, stream=stream)
-            so = eng.scene_offsets()
-            tp.append(time.perf_counter())
-            if self.keep_pairs:
-                if self.pinned[slot].shape[0] < total:
-                    self.pinned[slot] = torch.empty((int(total * 1.25) + 1024, 2), dtype=torch.int32).pin_memory()
-                buf = self.pinned[slot][:total]
-                eng.pairs_into(buf, stream=stream)
-                eng.sync(stream)
-                allp = buf.numpy().view(np.uint32)
-                if self.copy_pairs:  # the pinned buffer is reused by the slot's next batch
-                    allp = allp.copy()
+        items = (BatchItem * len(batch))()
+        keep = []  # arrays the native step reads
+        staged = total = 0
+        for i, (r, sc) in enumerate(zip(batch, scenes)):
+            r.nboxes = sc.host.shape[0]
+            upload = sc.dev is None
+            if upload:
+                self._place(sc, dev)
+            it = items[i]
+            it.dev = sc.dev.data_ptr()
+            it.host = sc.host.ctypes.data
+            it.n = sc.host.shape[0]
+            if r.kind == "update":
+                rows = np.ascontiguousarray(r.rows, dtype=np.uint32)
+                idx = np.ascontiguousarray(r.idx, dtype=np.uint32)
+                keep += [rows, idx]
+                it.rows, it.idx, it.k = rows.ctypes.data, idx.ctypes.data, idx.shape[0]
+                if not upload:
+                    staged += idx.shape[0]
+            it.upload = 1 if upload else 0
+            it.shift = sc.shift if sc.shift >= 0 else AUTO
+            total += sc.host.shape[0]
+        if self.staging[slot].shape[0] < staged:
+            self.staging[slot] = torch.empty((int(staged * 1.25) + 1024, 8), dtype=torch.int32).pin_memory()
+            self.stage_dev[slot] = torch.empty((int(staged * 1.25) + 1024, 8), dtype=torch.int32, device=dev)
+        if len(batch) > 1 and self.catbuf[slot].shape[0] < total:
+            self.catbuf[slot] = torch.empty((total, 7), dtype=torch.int32, device=dev)
         tp.append(time.perf_counter())
+        buf = self.pinned[slot]
+        rc, npairs, so, ph = eng.serve_batch(items, gen.RANGE, self.catbuf[slot].data_ptr(),
+                                             self.catbuf[slot].shape[0], self.staging[slot].data_ptr(),
+                                             self.stage_dev[slot].data_ptr(), self.staging[slot].shape[0],
+                                             stream, buf.data_ptr(), buf.shape[0])
+        if rc == ECAPACITY:  # more pairs than the slot's page-locked buffer holds: grow it, copy again
+            self.pinned[slot] = torch.empty((int(npairs * 1.25) + 1024, 2), dtype=torch.int32).pin_memory()
+            buf = self.pinned[slot]
+            eng.pairs_into(buf[:npairs], stream=stream)
+            eng.sync(stream)
+        tp.append(time.perf_counter())
+        allp = None
+        if self.keep_pairs:
+            allp = buf[:npairs].numpy().view(np.uint32)
+            if self.copy_pairs:  # the pinned buffer is reused by the slot's next batch
+                allp = allp.copy()
         t_done = self.now()
-        for i, r in enumerate(batch):
+        for i, (r, sc) in enumerate(zip(batch, scenes)):
+            sc.shift = int(items[i].shift)
             r.npairs = int(so[i + 1] - so[i])
             if self.keep_pairs:
                 r.pairs = allp[int(so[i]):int(so[i + 1])]
+            if self.keep_snapshots:
+                r.snapshot = sc.host.copy()
             r.done = t_done
             r.batch = self.batches
+        py_ms = (tp[1] - tp[0]) * 1e3
         with self.lock:
-            for k, name in enumerate(("prepare", "concat", "query", "download")):
-                if k + 1 < len(tp):
-                    self.phase_s[name] += tp[k + 1] - tp[k]
+            for name, v in zip(("prepare", "concat", "query", "download"), (py_ms + ph[0], ph[1], ph[2], ph[3])):
+                self.phase_s[name] += v * 1e-3
+            # (start s, boxes, requests, prepare, concat, query, download ms, Python part of the preparation ms)
             self.batch_log.append((t_start, sum(r.nboxes for r in batch), len(batch),
-                                   *[(tp[k + 1] - tp[k]) * 1e3 for k in range(len(tp) - 1)],
-                                   *[x * 1e3 for x in prep_split]))
+                                   py_ms + ph[0], ph[1], ph[2], ph[3], py_ms))
             self.batches += 1
             self.busy_time += t_done - t_start
             for sc in scenes:
@@ -328,55 +358,6 @@ class Server:
             self.done.extend(batch)
             self.free_slots.append(slot)
             self.lock.notify_all()
-
-    def _prepare(self, batch, scenes, dev, slot) -> None:
-        """Apply updates and make the batch's scenes device-resident (on the
-        current stream). The moved rows of every update in the batch go up
-        in one copy through the slot's page-locked staging buffer (free
-        again: the slot's previous batch ended with a stream synchronize)."""
-        torch = self.torch
-        moved = []  # (scene, indices) of updates whose scene stays resident
-        tt = [0.0, 0.0, 0.0, 0.0]  # host seconds: tuning, update rows, uploads, moved rows
-        for r, sc in zip(batch, scenes):
-            r.nboxes = sc.host.shape[0]
-            t0 = time.perf_counter()
-            if sc.shift < 0:  # first query of the scene: tune its cell size once
-                sc.shift = tune_shift(sc.host, gen.RANGE, 256)
-            t1 = time.perf_counter()
-            if r.kind == "update":  # the moved rows replace theirs in the host master copy
-                idx = r.idx
-                sc.host[idx] = r.rows
-                if sc.dev is not None:
-                    moved.append((sc, idx))
-            t2 = time.perf_counter()
-            if sc.dev is None:  # not on the device (new or dropped): upload it whole
-                self._upload(sc, dev)
-            t3 = time.perf_counter()
-            tt[0] += t1 - t0
-            tt[1] += t2 - t1
-            tt[2] += t3 - t2
-            if self.keep_snapshots:
-                r.snapshot = sc.host.copy()
-        t4 = time.perf_counter()
-        if moved:
-            k = sum(idx.shape[0] for _, idx in moved)
-            if self.staging[slot].shape[0] < k:
-                self.staging[slot] = torch.empty((int(k * 1.25) + 1024, 8), dtype=torch.int32).pin_memory()
-            st = self.staging[slot][:k].numpy()
-            a = 0
-            for sc, idx in moved:  # row = [7 coordinate/rid words, box index]
-                b = a + idx.shape[0]
-                np.take(sc.host.view(np.int32), idx, axis=0, out=st[a:b, :7])
-                st[a:b, 7] = idx.view(np.int32)
-                a = b
-            up = self.staging[slot][:k].to(dev, non_blocking=True)
-            a = 0
-            for sc, idx in moved:
-                b = a + idx.shape[0]
-                sc.dev.index_copy_(0, up[a:b, 7].long(), up[a:b, :7])
-                a = b
-        tt[3] = time.perf_counter() - t4
-        return tt
 
     # ---- dispatcher ----------------------------------------------------------
     def serve(self, n_expected: int, timeout: float = 600.0) -> None:
