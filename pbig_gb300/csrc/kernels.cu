@@ -327,11 +327,8 @@ constexpr int kScanTile = kScanChunk * kScanChunks;
 
 struct TileRec {                         // 64 bytes per tile
     unsigned long long sum;              // entries; exclusive prefix after k_scan_reduce
-    unsigned long long tests;            // pair tests of the tile's cells
     uint32_t chunk[kScanChunks];         // entries per chunk
-    unsigned long long comp;             // sum of n*n/2 over the tile's cells of n >= 2
-    uint32_t jobs;                       // sum of ceil(n/256) over them
-    uint32_t maxc;                       // largest of them
+    uint32_t pad[6];
 };
 static_assert(sizeof(TileRec) == 64, "tile record layout");
 
@@ -373,91 +370,48 @@ __device__ __forceinline__ void scan_load(const Params& p, uint64_t chunk, uint3
 
 __device__ __forceinline__ void reduce_chunk(TileRec* rec, uint64_t ch, const uint32_t v[kScanPerThread]) {
     const uint32_t lane = lane_id();
-    uint32_t lsum = 0, big = 0;  // < 2^32 while the entry total is
+    uint32_t lsum = 0;  // < 2^32 while the entry total is
 #pragma unroll
-    for (int k = 0; k < kScanPerThread; k++) {
-        lsum += v[k];
-        big |= v[k] >> 1;
-    }
+    for (int k = 0; k < kScanPerThread; k++) lsum += v[k];
     lsum = __reduce_add_sync(FULL_MASK, lsum);
     TileRec& r = rec[ch / kScanChunks];
     if (lane == 0) {
         r.chunk[ch % kScanChunks] = lsum;
         if (lsum) atomicAdd(&r.sum, (unsigned long long)lsum);
     }
-    if (__any_sync(FULL_MASK, big != 0)) {
-        unsigned long long tests = 0, comp = 0;
-        uint32_t jobs = 0, maxc = 0;
-#pragma unroll
-        for (int k = 0; k < kScanPerThread; k++) {
-            if (v[k] >= 2u) {
-                tests += (unsigned long long)v[k] * (v[k] - 1u) / 2u;
-                comp += (unsigned long long)v[k] * v[k] / 2u;
-                jobs += (v[k] + 255u) >> 8;
-                maxc = max(maxc, v[k]);
-            }
-        }
-        tests = warp_sum_u64(tests);
-        comp = warp_sum_u64(comp);
-        jobs = __reduce_add_sync(FULL_MASK, jobs);
-        maxc = __reduce_max_sync(FULL_MASK, maxc);
-        if (lane == 0 && tests) {
-            atomicAdd(&r.tests, tests);
-            atomicAdd(&r.comp, comp);
-            atomicAdd(&r.jobs, jobs);
-            atomicMax(&r.maxc, maxc);
-        }
-    }
 }
 
-// tile entry totals -> exclusive prefixes; the entry, pair-test and job
-// totals go to the counters. Run by one block of kReduceThreads threads,
-// kPrefixPer tiles per thread per round (4096 tiles in two rounds).
+// tile entry totals -> exclusive prefixes; the entry total goes to the
+// counters. Run by one block of kReduceThreads threads, kPrefixPer tiles per
+// thread per round (4096 tiles in two rounds).
 constexpr int kReduceThreads = kScanThreads;
 constexpr int kPrefixPer = 8;
 __device__ __forceinline__ void scan_prefix_block(const Params& p) {
-    __shared__ unsigned long long s_part[kReduceThreads / 32][4];
-    __shared__ unsigned long long s_carry[4];
+    __shared__ unsigned long long s_part[kReduceThreads / 32];
+    __shared__ unsigned long long s_carry;
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const uint64_t tiles = (p.ncells + kScanTile - 1) / kScanTile;
     TileRec* rec = reinterpret_cast<TileRec*>(p.tile_state);
-    if (t == 0) s_carry[0] = s_carry[1] = s_carry[2] = s_carry[3] = 0;
+    if (t == 0) s_carry = 0;
     // rounds of kPrefixPer tiles per thread: all loads of a round in flight
     // together; the records were written through L2 by other blocks (read
     // past L1)
     for (uint64_t r0 = 0; r0 < tiles; r0 += kPrefixPer * kReduceThreads) {
-        unsigned long long x[kPrefixPer], sx = 0, sy = 0, sc = 0, sj = 0, sm = 0;
+        unsigned long long x[kPrefixPer], sx = 0;
 #pragma unroll
         for (int k = 0; k < kPrefixPer; k++) {
             const uint64_t i = r0 + kPrefixPer * (uint64_t)t + k;
             x[k] = i < tiles ? __ldcg(&rec[i].sum) : 0ull;
             sx += x[k];
-            if (i < tiles) {
-                sy += __ldcg(&rec[i].tests);
-                sc += __ldcg(&rec[i].comp);
-                sj += __ldcg(&rec[i].jobs);
-                sm = max(sm, (unsigned long long)__ldcg(&rec[i].maxc));
-            }
         }
         const unsigned long long ix = warp_incl_scan64(sx);
-        const unsigned long long iy = warp_sum_u64(sy), ic = warp_sum_u64(sc), ij = warp_sum_u64(sj);
-        const unsigned long long im = __reduce_max_sync(FULL_MASK, (uint32_t)sm);
-        if (lane == 31) s_part[warp][0] = ix;
-        if (lane == 0) {
-            s_part[warp][1] = iy;
-            s_part[warp][2] = ic;
-            s_part[warp][3] = (ij << 32) | im;  // jobs < 2^32, max < 2^32
-        }
+        if (lane == 31) s_part[warp] = ix;
         __syncthreads();
-        unsigned long long wo = s_carry[0], tot = 0, tt = 0, tc = 0, tj = 0, tm = 0;
+        unsigned long long wo = s_carry, tot = 0;
         for (int w = 0; w < kReduceThreads / 32; w++) {
-            const unsigned long long a = s_part[w][0];
+            const unsigned long long a = s_part[w];
             if (w < (int)warp) wo += a;
             tot += a;
-            tt += s_part[w][1];
-            tc += s_part[w][2];
-            tj += s_part[w][3] >> 32;
-            tm = max(tm, s_part[w][3] & 0xffffffffull);
         }
         unsigned long long run = wo + (ix - sx);
 #pragma unroll
@@ -467,22 +421,12 @@ __device__ __forceinline__ void scan_prefix_block(const Params& p) {
             run += x[k];
         }
         __syncthreads();
-        if (t == 0) {
-            s_carry[0] += tot;
-            s_carry[1] += tt;
-            s_carry[2] += tc;
-            s_carry[3] = ((s_carry[3] >> 32) + tj) << 32 | max(s_carry[3] & 0xffffffffull, tm);
-        }
+        if (t == 0) s_carry += tot;
         __syncthreads();
     }
     if (t == 0) {
-        const unsigned long long total = s_carry[0];
-        p.ctr->entries = total;
-        p.ctr->tests = s_carry[1];
-        p.ctr->comp_pairs = s_carry[2];
-        p.ctr->jobs = s_carry[3] >> 32;
-        p.ctr->max_cell = (uint32_t)(s_carry[3] & 0xffffffffull);
-        if (total >= (1ull << 32)) atomicOr(&p.ctr->err, kErrEntryOvf);
+        p.ctr->entries = s_carry;
+        if (s_carry >= (1ull << 32)) atomicOr(&p.ctr->err, kErrEntryOvf);
     }
 }
 
@@ -573,6 +517,8 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_scan_cells(Params pin) {
     };
     issue(0);
     issue(1);
+    unsigned long long st_tests = 0;
+    uint32_t st_half = 0, st_jobs = 0, st_max = 0;
     for (uint64_t i = 0;; i++) {
         const uint64_t ch = first + i * nw;
         if (ch >= chunks) break;
@@ -673,9 +619,24 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_scan_cells(Params pin) {
                     const uint64_t idx = (uint64_t)b + rk;
                     const uint32_t key = p.records ? (uint32_t)(chunk_cell(ch, k >> 2) + (k & 3)) : st[k];
                     if (idx < pin.list_cap[c]) p.lists[pin.list_off[c] + idx] = make_uint2(key, v[k]);
+                    st_tests += (unsigned long long)v[k] * (v[k] - 1u) / 2u;
+                    st_half += v[k] >> 1;  // n*n/2 = n(n-1)/2 + n/2, rounded down
+                    st_jobs += (v[k] + 255u) >> 8;
+                    st_max = max(st_max, v[k]);
                 }
             }
         }
+    }
+    // the work statistics of this warp's cells (pair tests, and the
+    // reference's numCompPairs, 256-row jobs and largest cell)
+    st_tests = warp_sum_u64(st_tests);
+    const unsigned long long half = warp_sum_u64(st_half), jobs = warp_sum_u64(st_jobs);
+    st_max = __reduce_max_sync(FULL_MASK, st_max);
+    if (lane == 0 && st_max) {
+        atomicAdd(&p.ctr->tests, st_tests);
+        atomicAdd(&p.ctr->comp_pairs, st_tests + half);
+        atomicAdd(&p.ctr->jobs, jobs);
+        atomicMax(&p.ctr->max_cell, st_max);
     }
 }
 
