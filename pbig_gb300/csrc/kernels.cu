@@ -1074,9 +1074,13 @@ __device__ __forceinline__ void small_sweep(const Params& p, const Slots& s, War
     __syncwarp();
     const uint32_t gb = g * WG;
     const uint32_t nelm = r < n ? (r < (n >> 1) ? (n >> 1) : ((n - 1) >> 1)) : 0u;
+    // partners a lane of the warp needs at most: the sweep stops there rather
+    // than at WG/2 (a cell of 17 boxes in a 32-lane group needs 8, not 16)
+    const uint32_t dlim = __reduce_max_sync(FULL_MASK, nelm);
     uint32_t mask = 0;
 #pragma unroll
     for (uint32_t d = 1; d <= WG / 2; d++) {
+        if (d > dlim) break;
         uint32_t pr = r + d;
         if (pr >= n) pr -= n;
         if (pr >= WG) pr = 0;  // idle lanes (n = 0) stay inside the group
