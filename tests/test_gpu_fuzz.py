@@ -105,3 +105,31 @@ def test_random_batches(engine, seed):
     for i, b in enumerate(parts):
         want = O.brute_pairs(b) if len(b) else np.zeros((0, 2), np.uint32)
         assert np.array_equal(canon(res[int(so[i]):int(so[i + 1])]), want), (seed, i)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_merged_and_records(engine, seed):
+    """The same kind of scenes through the reference's merged build (sparse
+    cells merged into blocks, pbig.cu:1066-1251 and 223-318) and through its
+    Rice record stream (pbig.cu:788-920), decoded by the oracle's restatement
+    of decode.cc:38-131: both give the brute-force pair set."""
+    rs, dims, rng, n = scene_params(200 + seed)
+    boxes = random_scene(rs, max(n, 1), dims, rng)
+    want = O.brute_pairs(boxes)
+    engine.set_merged(True)
+    try:
+        got = engine.self_intersect(boxes, rng)
+        merged = canon(engine.pairs())
+    finally:
+        engine.set_merged(False)
+    assert got == len(want), seed
+    assert np.array_equal(merged, want), seed
+    engine.set_records(True)
+    try:
+        got = engine.self_intersect(boxes, rng)
+        words, start_i, recs = engine.records()
+    finally:
+        engine.set_records(False)
+    assert got == len(want), seed
+    dec = O.decode_rice(words, start_i, recs) if len(words) else np.zeros((0, 2), np.uint32)
+    assert np.array_equal(canon(dec), want), seed
