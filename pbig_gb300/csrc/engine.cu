@@ -807,23 +807,41 @@ PBIG2_API int pbig2_tune_shift(const uint32_t* boxes, uint64_t n, uint32_t dims,
 // autotuner with a per-context memo: a query whose size, dims, range and
 // mean box extent (over 256 strided boxes) match an earlier one within 5%
 // reuses that choice
-static TuneResult memo_tune(pbig2_ctx* c, const uint32_t* boxes, uint64_t n_avail, uint64_t n, int dims,
-                            uint32_t range, uint64_t sample) {
+constexpr uint64_t kMemoRows = 256;
+
+static double mean_extent(const uint32_t* boxes, uint64_t n_avail, int dims) {
     const int W = 2 * dims + 1;
-    const uint64_t m = std::min<uint64_t>(n_avail, 256);
+    const uint64_t m = std::min<uint64_t>(n_avail, kMemoRows);
     double ext = 0;
     for (uint64_t i = 0; i < m; i++) {
         const uint32_t* b = boxes + (uint64_t)((unsigned __int128)i * n_avail / m) * W;
         for (int d = 0; d < dims; d++) ext += (double)b[2 * d + 1] - (double)b[2 * d];
     }
-    ext = m ? ext / (double)(m * dims) : 0;
+    return m ? ext / (double)(m * dims) : 0;
+}
+
+static bool memo_find(pbig2_ctx* c, uint64_t n, int dims, uint32_t range, double ext, TuneResult& tr) {
     for (const auto& e : c->memo)
         if (e.dims == dims && e.range == range && std::fabs((double)e.n - (double)n) <= 0.05 * (double)n &&
-            std::fabs(e.ext - ext) <= 0.05 * std::max(1.0, e.ext))
-            return TuneResult{e.shift, e.est_e * (double)n / std::max(1.0, (double)e.n), 0, 0};
-    TuneResult tr = tune_shift_sample(boxes, n_avail, n, dims, range, sample);
+            std::fabs(e.ext - ext) <= 0.05 * std::max(1.0, e.ext)) {
+            tr = TuneResult{e.shift, e.est_e * (double)n / std::max(1.0, (double)e.n), 0, 0};
+            return true;
+        }
+    return false;
+}
+
+static void memo_put(pbig2_ctx* c, uint64_t n, int dims, uint32_t range, double ext, const TuneResult& tr) {
     if (c->memo.size() >= 64) c->memo.erase(c->memo.begin());
     c->memo.push_back({n, dims, range, ext, tr.shift, tr.est_entries});
+}
+
+static TuneResult memo_tune(pbig2_ctx* c, const uint32_t* boxes, uint64_t n_avail, uint64_t n, int dims,
+                            uint32_t range, uint64_t sample) {
+    const double ext = mean_extent(boxes, n_avail, dims);
+    TuneResult tr{};
+    if (memo_find(c, n, dims, range, ext, tr)) return tr;
+    tr = tune_shift_sample(boxes, n_avail, n, dims, range, sample);
+    memo_put(c, n, dims, range, ext, tr);
     return tr;
 }
 
@@ -874,11 +892,20 @@ static int self_or_bip(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const 
                 const uint32_t* src = g < n_red ? red + g * W : blue + (g - n_red) * W;
                 memcpy(&smp[i * W], src, W * 4);
             }
+            tr = memo_tune(c, smp.data(), smp.size() / W, n, (int)dims, range, kSample);
         } else {
-            int rc = sample_device_boxes(c, d_boxes, n, (int)dims, kSample, st, smp);
+            // device-resident boxes: 256 rows recognise a remembered scene;
+            // the full sample crosses to the host only when none matches
+            int rc = sample_device_boxes(c, d_boxes, n, (int)dims, kMemoRows, st, smp);
             if (rc) return rc;
+            const double ext = mean_extent(smp.data(), smp.size() / W, (int)dims);
+            if (!memo_find(c, n, (int)dims, range, ext, tr)) {
+                rc = sample_device_boxes(c, d_boxes, n, (int)dims, kSample, st, smp);
+                if (rc) return rc;
+                tr = tune_shift_sample(smp.data(), smp.size() / W, n, (int)dims, range, kSample);
+                memo_put(c, n, (int)dims, range, ext, tr);
+            }
         }
-        tr = memo_tune(c, smp.data(), smp.size() / W, n, (int)dims, range, kSample);
     }
     std::vector<GridScene> sc;
     if (!bip) {
