@@ -301,17 +301,18 @@ __global__ void __launch_bounds__(kBoxThreads) k_scatter(Params pin) {
 // flight together. Tile records (64 bytes, zeroed before the scan) collect
 // per-chunk entry sums and per-tile totals.
 //
-//   k_scan_reduce  chunk entry total (stored per chunk, added to the tile)
-//                  and the pair tests of its cells (added to the tile);
+//   k_scan_reduce  chunk entry total (stored per chunk, added to the tile);
 //                  two chunks per warp iteration, so eight 16-byte loads
 //                  per lane are in flight together. The last block to
 //                  finish turns the tile entry totals into exclusive
-//                  prefixes; the entry and pair-test totals go to the
-//                  counters.
+//                  prefixes; the entry total goes to the counters.
 //   k_scan_cells   the same chunks again: starts from the tile prefix, the
 //                  tile's earlier chunks and a warp scan; every cell of two
 //                  or more boxes goes to its work list, a chunk reserving
-//                  its places with one atomic per list (list order is free).
+//                  its places with one atomic per list (list order is free);
+//                  each warp sums the work statistics of its cells (pair
+//                  tests, numCompPairs, 256-row jobs, largest cell) and adds
+//                  them to the counters once.
 //
 // Lane l of a warp owns the 4 cells at 4l of each of the chunk's 4 rows of
 // 128 cells, so each 16-byte load or store of a warp covers 512 contiguous
