@@ -673,9 +673,10 @@ __global__ void k_expand(Params p) {
 //                  staged whole in the warp's shared memory
 //   k_pairs_block  cells of kMedMax+1..kBigMax boxes staged whole by a
 //                  block, and 32x32 tile tasks of larger cells
-// Warp items run independently (no block barriers); each warp compacts its
-// pairs into its own shared-memory buffer and flushes it to the pair array
-// with one global reservation per flush.
+// The warp items of the small- and medium-cell kernels run independently (no
+// block barriers); each warp compacts its pairs into its own shared-memory
+// buffer and flushes it to the pair array with one global reservation per
+// flush (the block kernel does the same per block).
 //
 // The test of one (row box, column box) pair is branch free: with every
 // coordinate < 2^29 the six differences max-min are non-negative exactly
