@@ -353,6 +353,7 @@ static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t nc
         if (cudaEventElapsedTime(&x, c->evp[7], c->evp[8]) == cudaSuccess) phase[7] = std::max(0.f, x);
         if (cudaEventElapsedTime(&x, c->evp[8], c->evp[5]) == cudaSuccess) phase[8] = std::max(0.f, x);
     }
+    c->last_err = h.err;
     pbig2_stats& s = c->stats;
     s.boxes = nboxes;
     s.bad_boxes = h.bad;
@@ -487,6 +488,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
                         const std::vector<GridScene>& scenes, uint32_t split, double est_entries,
                         cudaStream_t st, bool group) {
     const uint32_t nsc = (uint32_t)scenes.size();
+    c->last_err = 0;
     if (nboxes > (uint64_t)kIdMask + 1)
         return fail(PBIG2_EINVAL, "a query holds at most 2^29 boxes (got %llu)", (unsigned long long)nboxes);
     // scene table
@@ -845,6 +847,20 @@ static TuneResult memo_tune(pbig2_ctx* c, const uint32_t* boxes, uint64_t n_avai
     return tr;
 }
 
+// A box outside the tuner's sample can cover 2^26 cells or more at the cell
+// size chosen from the sample; the count kernel then skips it as an input
+// error (kErrCellOvf). A query whose cell sizes were chosen automatically is
+// then run again on grids twice as coarse per axis, until every box fits.
+static bool coarser_grid_helps(const pbig2_ctx* c, int rc) {
+    return rc == PBIG2_EINPUT && (c->last_err & kErrCellOvf) != 0;
+}
+
+// later queries of a remembered scene start at the cell size that fitted
+static void memo_raise(pbig2_ctx* c, uint64_t n, int dims, uint32_t range, uint32_t from, uint32_t to) {
+    for (auto& e : c->memo)
+        if (e.n == n && e.dims == dims && e.range == range && e.shift == from) e.shift = to;
+}
+
 static int self_or_bip(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const uint32_t* blue, uint64_t n_blue,
                        uint32_t dims, uint32_t range, uint32_t cell_shift, int loc, void* stream, uint64_t* npairs) {
     if (!c || !npairs || (dims != 2 && dims != 3) || range == 0) return fail(PBIG2_EINVAL, "bad arguments");
@@ -921,6 +937,16 @@ static int self_or_bip(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const 
     }
     int rc = run_pipeline(c, d_boxes, n, (int)dims, range, sc, bip ? (uint32_t)n_red : kNoSplit,
                           std::max(tr.est_entries, (double)n), st, false);
+    if (cell_shift == PBIG2_AUTO && coarser_grid_helps(c, rc)) {
+        const uint32_t first = tr.shift;
+        while (coarser_grid_helps(c, rc) && tr.shift < 31) {
+            tr.shift++;
+            for (auto& g : sc) g.shift = tr.shift;
+            rc = run_pipeline(c, d_boxes, n, (int)dims, range, sc, bip ? (uint32_t)n_red : kNoSplit,
+                              std::max(tr.est_entries, (double)n), st, false);
+        }
+        memo_raise(c, n, (int)dims, range, first, tr.shift);
+    }
     c->up_red = c->up_blue = nullptr;
     *npairs = c->npairs;
     return rc;
@@ -998,6 +1024,18 @@ PBIG2_API int pbig2_batch_intersect(pbig2_ctx* c, const uint32_t* boxes, const u
         est_e += e;
     }
     rc = run_pipeline(c, d_boxes, n, (int)dims, range, sc, kNoSplit, est_e, st, true);
+    // automatic cell sizes: coarser grids for every scene while a box does
+    // not fit (the failing scene is not known)
+    while (!cell_shifts && coarser_grid_helps(c, rc)) {
+        bool raised = false;
+        for (auto& g : sc)
+            if (g.shift < 31) {
+                g.shift++;
+                raised = true;
+            }
+        if (!raised) break;
+        rc = run_pipeline(c, d_boxes, n, (int)dims, range, sc, kNoSplit, est_e, st, true);
+    }
     *npairs = c->npairs;
     return rc;
 }

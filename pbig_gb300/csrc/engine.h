@@ -60,6 +60,7 @@ struct pbig2_ctx {
     uint64_t rice_words = 0;     // words of the last record stream
     uint64_t last_ncells = 0, last_entries = 0;
     uint32_t merged_blocks = 0;  // merged blocks of the last query
+    uint32_t last_err = 0;       // error bits of the last pipeline pass
     pbig::DevBuf d_boxes, d_counts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
         d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims, d_scene_tab;
     pbig::HostPinned h_ctr, h_stage;
