@@ -165,19 +165,27 @@ static TuneResult tune_impl(const uint32_t* boxes, const std::vector<uint64_t>& 
     std::vector<uint64_t> keys;
     std::vector<uint32_t> cnts;
     double best_cost = 1e300;
-    for (int s = std::max(0, s0 - 2); s <= std::min(31, s0 + 3); s++) {
+    // candidates: s0-2 .. s0+3; only when none of those qualifies (a few
+    // huge boxes in the sample can disqualify them all), every coarser size,
+    // the cheapest by the cost model
+    const int s_win = std::min(31, s0 + 3);
+    for (int s = std::max(0, s0 - 2); s <= 31; s++) {
+        if (s == s_win + 1 && best_cost < 1e300) break;
         const uint32_t nrc = nrc_for(range, (uint32_t)s);
         const double C = std::pow((double)nrc, dims);
         if (C > 4.0e9) continue;
-        double E = 0;
+        if (s > s_win && C > std::max(4096.0, 64.0 * (double)n)) continue;  // widened: grids in proportion to n
+        double E = 0, cmax = 0;
         for (uint64_t i : idx) {
             const uint32_t* b = boxes + i * W;
             if (!box_ok(b, dims, range)) continue;
             double c = 1;
             for (int d = 0; d < dims; d++) c *= (double)((b[2 * d + 1] >> s) - (b[2 * d] >> s) + 1);
             E += c;
+            cmax = std::max(cmax, c);
         }
         if (E / (double)idx.size() > 64.0) continue;  // replication too high to be a candidate
+        if (cmax >= (double)(1u << 26)) continue;     // a sampled box would not fit (2^26 cells or more)
         const double Es = E;
         E *= scale;
         double T;
