@@ -64,7 +64,9 @@ typedef struct {
     uint32_t cell_shift;   /* log2(cell size) of the (first) scene */
     uint32_t scenes;
     uint32_t kernels;      /* kernel launches of the query */
-    uint32_t reserved;
+    uint32_t grid_retries; /* automatic cell size: passes rerun on a coarser
+                              grid because a box outside the tuner's sample
+                              covered 2^26 cells or more */
     double device_ms;      /* device time of the query (CUDA events) */
     /* device time per phase of the last pipeline pass (CUDA events on the
      * query's stream): count, scan, expand, scatter, pair test (all three
@@ -249,8 +251,10 @@ PBIG2_API int pbig2_serve_batch(pbig2_ctx* ctx, pbig2_batch_item* items, uint32_
  * 524288 box-in-cell entries; larger queries return PBIG2_ECAPACITY. The
  * scratch is shared by all calls, so calls that overlap on the GPU race; the
  * first call on a device sets the device up and should come before any
- * stream capture. *npairs receives the pair count (also when the pair
- * buffer is too small). Error text: pbig2_noalloc_last_error(). */
+ * stream capture. d_pairs must be 8-byte aligned (PBIG2_EINVAL otherwise).
+ * *npairs receives the pair count, also when the pair buffer is too small;
+ * it is 0 when the scene needs more cell entries than the scratch holds.
+ * Error text: pbig2_noalloc_last_error(). */
 PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, uint32_t dims, uint32_t range,
                                            uint32_t cell_shift, uint32_t* d_pairs, uint64_t pair_cap,
                                            uint64_t* npairs, void* stream);
@@ -286,6 +290,12 @@ PBIG2_API int pbig2_scene_boxes(pbig2_scene* scene, const uint32_t** boxes, uint
 /* Copy the first count pairs of the full list (which = 0), the removed
  * (1) or the added (2) pairs of the last move into dst (host or device). */
 PBIG2_API int pbig2_scene_copy(pbig2_scene* scene, int which, uint32_t* dst, uint64_t count);
+
+/* Cells of the grid a query at cell size 2^shift uses over [0, range) in
+ * dims dimensions: ceil(range / 2^shift)^dims, saturating at UINT64_MAX
+ * (no counterpart in the reference, whose 32-bit nCells wraps). Queries
+ * refuse grids of 2^32 - 1 cells or more. */
+PBIG2_API uint64_t pbig2_grid_cells(uint32_t range, uint32_t shift, uint32_t dims);
 
 /* Cell-size autotuner: the shift the engine would pick for these boxes
  * (host memory), from a sample of at most `sample` boxes. */

@@ -376,6 +376,7 @@ static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t nc
     s.cell_shift = scenes.empty() ? 0 : scenes[0].shift;
     s.scenes = nsc;
     s.kernels = (uint32_t)launches;
+    s.grid_retries = 0;  // set by the caller after a coarser-grid rerun
     s.device_ms = ms;
     for (int k = 0; k < 9; k++) s.phase_ms[k] = phase[k];
     (void)cudaGetLastError();  // a timing query on an unrecorded event is not an error of the query
@@ -514,9 +515,8 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         s.pad = 0;
         if (g.grid_of == (int)i) {
             s.cell_off = ncells;
-            uint64_t cc = s.nrc;
-            for (int d = 1; d < dims; d++) cc *= s.nrc;
-            ncells += cc;
+            const uint64_t cc = grid_cells(range, g.shift, dims);  // saturating
+            ncells = cc > ~0ull - ncells ? ~0ull : ncells + cc;
         } else {
             s.cell_off = tab[g.grid_of].cell_off;
         }
@@ -807,6 +807,10 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     return PBIG2_OK;
 }
 
+PBIG2_API uint64_t pbig2_grid_cells(uint32_t range, uint32_t shift, uint32_t dims) {
+    return grid_cells(range, shift, (int)dims);
+}
+
 PBIG2_API int pbig2_tune_shift(const uint32_t* boxes, uint64_t n, uint32_t dims, uint32_t range, uint64_t sample,
                                uint32_t* shift) {
     if (!boxes || !shift || (dims != 2 && dims != 3) || range == 0) return fail(PBIG2_EINVAL, "bad arguments");
@@ -954,6 +958,7 @@ static int self_or_bip(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const 
                               std::max(tr.est_entries, (double)n), st, false);
         }
         memo_raise(c, n, (int)dims, range, first, tr.shift);
+        c->stats.grid_retries = tr.shift - first;
     }
     c->up_red = c->up_blue = nullptr;
     *npairs = c->npairs;
@@ -1034,6 +1039,7 @@ PBIG2_API int pbig2_batch_intersect(pbig2_ctx* c, const uint32_t* boxes, const u
     rc = run_pipeline(c, d_boxes, n, (int)dims, range, sc, kNoSplit, est_e, st, true);
     // automatic cell sizes: coarser grids for every scene while a box does
     // not fit (the failing scene is not known)
+    uint32_t retries = 0;
     while (!cell_shifts && coarser_grid_helps(c, rc)) {
         bool raised = false;
         for (auto& g : sc)
@@ -1043,7 +1049,9 @@ PBIG2_API int pbig2_batch_intersect(pbig2_ctx* c, const uint32_t* boxes, const u
             }
         if (!raised) break;
         rc = run_pipeline(c, d_boxes, n, (int)dims, range, sc, kNoSplit, est_e, st, true);
+        retries++;
     }
+    c->stats.grid_retries = retries;
     *npairs = c->npairs;
     return rc;
 }

@@ -33,6 +33,19 @@ constexpr int kListMed = 4, kListBig = 5, kListHuge = 6;
 constexpr uint32_t kMedMax = 128;   // largest cell staged by one warp
 constexpr uint32_t kBigMax = 512;   // largest cell staged by one block
 
+// cells of a dims-D grid with ceil(range / 2^shift) cells per axis,
+// saturating at UINT64_MAX (in 3-D a fine grid over a wide range has more
+// than 2^64 cells: range 2^32 at shift 0 gives 2^96)
+__host__ __device__ inline uint64_t grid_cells(uint32_t range, uint32_t shift, int dims) {
+    const uint64_t nrc = shift >= 32 ? (range ? 1u : 0u) : (((uint64_t)range + (1ull << shift) - 1) >> shift);
+    uint64_t c = nrc;
+    for (int d = 1; d < dims; d++) {
+        if (nrc && c > ~0ull / nrc) return ~0ull;
+        c *= nrc;
+    }
+    return c;
+}
+
 struct Scene {
     uint32_t box_off;   // first box of the scene (global index)
     uint32_t n;         // boxes in the scene

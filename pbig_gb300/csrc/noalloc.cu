@@ -21,6 +21,7 @@
 // The first call on a device does that device's set-up (the scratch
 // address via cudaGetSymbolAddress and the kernels' shared-memory limits);
 // make that first call before any stream capture.
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -69,6 +70,8 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
     if (!npairs || (dims != 2 && dims != 3) || range == 0 || (n && !d_boxes) || (pair_cap && !d_pairs))
         return na_fail(PBIG2_EINVAL, "bad arguments");
     *npairs = 0;
+    // the pair kernels store 8- and 16-byte units into the pair buffer
+    if (((uintptr_t)d_pairs & 7u) != 0) return na_fail(PBIG2_EINVAL, "d_pairs must be 8-byte aligned");
     if (n > kNaMaxBoxes) return na_fail(PBIG2_ECAPACITY, "more than 262144 boxes: use pbig2_self_intersect");
     if (cell_shift != PBIG2_AUTO && cell_shift > 31) return na_fail(PBIG2_EINVAL, "cell_shift > 31");
     int dev = 0;
@@ -111,15 +114,14 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
         shift = 0;
         while (shift < 31 && (double)(1u << (shift + 1)) <= ext) shift++;
     }
-    auto cells_for = [&](uint32_t s) {
-        const uint64_t nrc = ((uint64_t)range + (1ull << s) - 1) >> s;
-        uint64_t c = nrc;
-        for (uint32_t d = 1; d < dims; d++) c *= nrc;
-        return c;
-    };
-    while (shift < 31 && cells_for(shift) > kNaMaxCells) shift++;
-    const uint64_t ncells = cells_for(shift);
+    // grid_cells saturates: a fine grid over a wide range (3-D, shift 0,
+    // range 2^24: 2^72 cells) must not wrap to a small count
+    while (shift < 31 && grid_cells(range, shift, (int)dims) > kNaMaxCells) shift++;
+    const uint64_t ncells = grid_cells(range, shift, (int)dims);
     if (ncells > kNaMaxCells) return na_fail(PBIG2_ECAPACITY, "grid does not fit the scratch");
+    // with at most 2^20 cells in the grid no box can cover the 2^26 cells at
+    // which the count skips it, so unlike pbig2_self_intersect this entry
+    // point never needs a coarser retry
 
     // carve the scratch
     unsigned char* base = (unsigned char*)g_scratch_ptr[dev];
@@ -184,8 +186,9 @@ PBIG2_API int pbig2_self_intersect_noalloc(const uint32_t* d_boxes, uint64_t n, 
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return na_fail(PBIG2_ECUDA, "pipeline", e);
-    *npairs = h.pairs;
+    // an entry or task overflow leaves the pair count meaningless: *npairs stays 0
     if (h.err & (kErrEntryOvf | kErrTaskOvf)) return na_fail(PBIG2_ECAPACITY, "scene needs more cell entries than the scratch holds (limit 524288)");
+    *npairs = h.pairs;
     if (h.err & kErrWait) return na_fail(PBIG2_ETIMEOUT, "a bounded device wait gave up (scan bulk copy)");
     if (h.err & kErrIndex) return na_fail(PBIG2_ECUDA, "inconsistent cell lists");
     if (h.pairs > pair_cap) return na_fail(PBIG2_ECAPACITY, "pair buffer too small; *npairs holds the pair count");

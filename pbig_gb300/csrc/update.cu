@@ -531,7 +531,7 @@ PBIG2_API int pbig2_scene_create(pbig2_ctx* c, const uint32_t* boxes, uint64_t n
     s->shift = st.cell_shift;
     s->nrc = nrc_for(range, s->shift);
     s->n = n;
-    s->ncells = (uint64_t)s->nrc * s->nrc * (dims == 3 ? s->nrc : 1u);
+    s->ncells = grid_cells(range, s->shift, (int)dims);  // below 2^32: the query above ran on this grid
     cudaStream_t sm = c->own_stream;
     const int W = 2 * (int)dims + 1;
     auto bail = [&](int code) {

@@ -32,6 +32,7 @@ EXPORTS = [
     "pbig2_noalloc_last_error", "pbig2_set_option", "pbig2_scene_create", "pbig2_scene_destroy",
     "pbig2_scene_move", "pbig2_scene_delta", "pbig2_scene_pairs", "pbig2_scene_boxes", "pbig2_scene_copy",
     "pbig2_result_records", "pbig2_copy_records", "pbig2_decode_records", "pbig2_serve_batch",
+    "pbig2_grid_cells",
 ]
 
 
@@ -51,14 +52,14 @@ class Stats(C.Structure):
     _fields_ = [("boxes", C.c_uint64), ("bad_boxes", C.c_uint64), ("cells", C.c_uint64),
                 ("entries", C.c_uint64), ("pair_tests", C.c_uint64), ("pairs", C.c_uint64),
                 ("cell_shift", C.c_uint32), ("scenes", C.c_uint32), ("kernels", C.c_uint32),
-                ("reserved", C.c_uint32), ("device_ms", C.c_double), ("phase_ms", C.c_double * 9),
+                ("grid_retries", C.c_uint32), ("device_ms", C.c_double), ("phase_ms", C.c_double * 9),
                 ("comp_pairs", C.c_uint64), ("jobs", C.c_uint64), ("max_cell", C.c_uint32),
                 ("merged_blocks", C.c_uint32)]
 
     PHASES = ("count", "scan", "expand", "scatter", "pairs", "group", "pairs_small", "pairs_med", "pairs_block")
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("reserved", "phase_ms")}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "phase_ms"}
         d["phase_ms"] = dict(zip(self.PHASES, list(self.phase_ms)))
         return d
 
@@ -99,6 +100,8 @@ def lib():
         L.pbig2_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
         L.pbig2_host_free.argtypes = [vp]
         L.pbig2_tune_shift.argtypes = [vp, u64, u32, u32, u64, C.POINTER(u32)]
+        L.pbig2_grid_cells.argtypes = [u32, u32, u32]
+        L.pbig2_grid_cells.restype = u64
         L.pbig2_self_intersect_noalloc.argtypes = [vp, u64, u32, u32, u32, vp, u64, C.POINTER(u64), vp]
         L.pbig2_noalloc_last_error.restype = C.c_char_p
         L.pbig2_set_option.argtypes = [vp, C.c_int, C.c_int64]

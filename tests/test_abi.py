@@ -10,7 +10,8 @@ import pytest
 from pbig_gb300 import build, engine
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+# the reference project's source tree (awatch/pbig), when a copy is at hand
+REF = os.environ.get("PBIG_REFERENCE_DIR", "")
 
 
 def _declared(header):
@@ -26,6 +27,23 @@ def test_engine_library_exports_every_declared_symbol():
     for n in names:
         assert hasattr(lib, n), n
     assert sorted(engine.EXPORTS) == names
+
+
+def test_grid_cells_saturates():
+    """Cell counts of fine grids over wide ranges do not wrap: in 3-D at range
+    2^24, shifts 0, 1 and 2 give 2^72, 2^69 and 2^66 cells."""
+    f = engine.lib().pbig2_grid_cells
+    big = (1 << 64) - 1
+    for shift in (0, 1, 2):
+        assert f(1 << 24, shift, 3) == big
+    assert f(1 << 24, 0, 3) > 1 << 32
+    assert f(1 << 24, 3, 3) == 1 << 63
+    assert f(1 << 24, 16, 3) == 256 ** 3
+    assert f(0xFFFFFFFF, 0, 2) == 0xFFFFFFFF ** 2
+    assert f(0xFFFFFFFF, 0, 3) == big
+    assert f(1000, 3, 2) == 125 * 125
+    assert f(1000, 31, 3) == 1
+    assert f(1 << 24, 22, 3) == 64
 
 
 def test_legacy_archive_exports_mangled_api():
@@ -44,7 +62,7 @@ def test_legacy_client_builds(tmp_path):
         assert os.path.exists(exe)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(REF), reason="PBIG_REFERENCE_DIR not set")
 def test_reference_example_client_links_unchanged(tmp_path):
     """package/main.cc + package/report.cc of the reference, unmodified,
     against this library (the shim is compiled with the package's report.h)."""
@@ -54,7 +72,7 @@ def test_reference_example_client_links_unchanged(tmp_path):
     assert os.path.exists(exe)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(REF), reason="PBIG_REFERENCE_DIR not set")
 def test_reference_harness_links_unchanged(tmp_path):
     """src/pbig/main.cc + hybrid.cc + report.cc (check.PBIG) link against the
     library, using its device_init/pbig_* symbols."""

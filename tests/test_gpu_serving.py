@@ -1,7 +1,8 @@
 """The serving loop: continuous batching of scene queries and updates.
 
-Each request's pair set must be the same as that of the scene (as it was
-when the request ran) queried alone, whatever batch it was mixed into.
+Each request's pair set, whatever batch it was mixed into, must equal the
+oracle's pairs of the scene as it was when the request ran, and the pairs of
+that scene queried alone on the engine.
 """
 import numpy as np
 import pytest
@@ -15,9 +16,13 @@ pytestmark = pytest.mark.gpu
 def _check_alone(engine, reqs):
     for r in reqs:
         assert r.done > 0, r.rid
+        want, _ = O.grid_pairs(r.snapshot, gen.RANGE)
+        got = O.sort_pairs(r.pairs)
+        assert r.npairs == len(want), r.rid
+        assert np.array_equal(got, want), r.rid
         n = engine.self_intersect(r.snapshot, gen.RANGE)
         assert n == r.npairs
-        assert np.array_equal(O.sort_pairs(r.pairs), O.sort_pairs(engine.pairs())), r.rid
+        assert np.array_equal(O.sort_pairs(engine.pairs()), want), r.rid
 
 
 def test_serving_results_equal_alone_and_in_the_mix(engine):
