@@ -114,7 +114,9 @@ PBIG2_API int pbig2_bipartite_intersect(pbig2_ctx* ctx, const uint32_t* red, uin
  * 0); scene_offsets has n_scenes+1 entries (host memory). Pairs are grouped
  * by scene: scene s owns result pairs [pair_offsets[s], pair_offsets[s+1])
  * with scene-local indices (pbig2_result_scene_offsets). cell_shifts may be
- * NULL (autotune every scene) or hold one shift per scene. */
+ * NULL (every scene's cell size is chosen on the device, one warp per scene
+ * running the autotuner's cost model on up to 64 of its boxes) or hold one
+ * shift per scene. */
 PBIG2_API int pbig2_batch_intersect(pbig2_ctx* ctx, const uint32_t* boxes,
                                     const uint64_t* scene_offsets, uint32_t n_scenes, uint32_t dims,
                                     uint32_t range, const uint32_t* cell_shifts, int boxes_loc,
@@ -161,6 +163,12 @@ PBIG2_API int pbig2_copy_pairs(pbig2_ctx* ctx, uint32_t* dst, uint64_t first, ui
 /* Per-scene pair offsets of the last batched query (n_scenes+1 values,
  * host memory). */
 PBIG2_API int pbig2_result_scene_offsets(pbig2_ctx* ctx, uint64_t* offsets, uint32_t n_scenes);
+
+/* Cell size (log2) each scene of the last query ran with: n_scenes values
+ * for a batched query, 1 for a self or red/blue query (host memory). With
+ * automatic cell sizes these are the autotuner's choices, after any coarser
+ * rerun (pbig2_stats.grid_retries). */
+PBIG2_API int pbig2_result_scene_shifts(pbig2_ctx* ctx, uint32_t* shifts, uint32_t n_scenes);
 
 /* Asynchronous variant of pbig2_copy_pairs: enqueues the copy on `stream`
  * and returns; pbig2_sync waits for it. */

@@ -72,8 +72,9 @@ def _engine_cmds(extra: list[str]) -> tuple[list[list[str]], list[str]]:
     for src in ENGINE_SOURCES:
         obj = os.path.join(BUILD, src + ".o")
         objs.append(obj)
+        # -ffp-contract=off: the host autotuner rounds like its device twin
         cmds.append([NVCC, *ARCH_FLAGS, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-Xcompiler", "-fvisibility=hidden", "-I", INCLUDE, "-I", CSRC,
+                     "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC,
                      *extra, "-c", os.path.join(CSRC, src), "-o", obj])
     return cmds, objs
 

@@ -86,19 +86,20 @@ uint32_t nrc_for(uint32_t range, uint32_t shift) {
 
 // --------------------------------------------------------------------------
 // autotuner: cost(s) = kCell*C(s) + kEntry*E(s) + kTest*T(s) in seconds
-// (C cells, E box-in-cell entries, T pair tests), estimated from a sample.
-// T is counted exactly on the sample (cell occupancy by hashing) and scaled
-// by (n/m)^2, since a pair of boxes survives sampling with probability
-// (m/n)^2. A test costs more once the tests sit in cells beyond the
-// medium-cell kernel's reach: with the entry-weighted mean occupancy
-// m = 2T/E + 1, kTest is scaled by max(1, m / kOccTest). The constants are
-// fitted on GB300 cell-size sweeps (2-D/3-D, uniform/clustered, single
-// scenes and a 4096-scene batch), where they pick the fastest size or one
-// within 2%; per unit, an entry costs ~16 ps in the count and scatter plus
-// its fetch and sweep in the pair kernels, a test ~1 ps in the medium-cell
-// kernel and ~2 ps in the block kernel.
+// (C cells, E box-in-cell entries, T pair tests; tune_cost in kernels.cuh),
+// estimated from a sample. T is counted exactly on the sample (cell
+// occupancy by hashing) and scaled by (n/m)^2, since a pair of boxes
+// survives sampling with probability (m/n)^2. A test costs more once the
+// tests sit in cells beyond the medium-cell kernel's reach: with the
+// entry-weighted mean occupancy m = 2T/E + 1, kTest is scaled by
+// max(1, m / kOccTest). The constants are fitted on GB300 cell-size sweeps
+// (2-D/3-D, uniform/clustered, single scenes and a 4096-scene batch), where
+// they pick the fastest size or one within 2%; per unit, an entry costs
+// ~16 ps in the count and scatter plus its fetch and sweep in the pair
+// kernels, a test ~1 ps in the medium-cell kernel and ~2 ps in the block
+// kernel. Batched queries run the same model on the device, one warp per
+// scene, with T = E^2 / 2C (k_tune_scenes).
 // --------------------------------------------------------------------------
-static const double kCell = 2.4e-12, kEntry = 80.0e-12, kTest = 0.9e-12, kOccTest = 96.0;
 
 // pair tests of the sample at one cell size: occupancy of the sample's cells
 // counted in an open-addressing hash table (key = cell id + 1)
@@ -142,7 +143,7 @@ static bool box_ok(const uint32_t* b, int dims, uint32_t range) {
 
 // n is the number of boxes the sample idx stands for
 static TuneResult tune_impl(const uint32_t* boxes, const std::vector<uint64_t>& idx, uint64_t n, int dims,
-                            uint32_t range, bool exact_tests) {
+                            uint32_t range) {
     const int W = 2 * dims + 1;
     TuneResult best{0, 0, 0, 0};
     if (idx.empty()) {
@@ -150,17 +151,14 @@ static TuneResult tune_impl(const uint32_t* boxes, const std::vector<uint64_t>& 
         while (best.shift > 0 && nrc_for(range, best.shift - 1) <= 1) best.shift--;
         return best;
     }
-    double mean_ext = 0;
-    uint64_t good = 0;
+    uint64_t ext_sum = 0, good = 0;  // exact: the device tuner sums the same integers
     for (uint64_t i : idx) {
         const uint32_t* b = boxes + i * W;
         if (!box_ok(b, dims, range)) continue;
-        for (int d = 0; d < dims; d++) mean_ext += (double)(b[2 * d + 1] - b[2 * d]) + 1.0;
+        for (int d = 0; d < dims; d++) ext_sum += (uint64_t)(b[2 * d + 1] - b[2 * d]) + 1;
         good++;
     }
-    if (good == 0) good = 1;
-    mean_ext /= (double)(good * dims);
-    int s0 = (int)std::floor(std::log2(std::max(1.0, mean_ext)));
+    const int s0 = tune_s0(ext_sum, (good ? good : 1) * (uint64_t)dims);
     const double scale = (double)n / (double)idx.size();
     std::vector<uint64_t> keys;
     std::vector<uint32_t> cnts;
@@ -172,7 +170,7 @@ static TuneResult tune_impl(const uint32_t* boxes, const std::vector<uint64_t>& 
     for (int s = std::max(0, s0 - 2); s <= 31; s++) {
         if (s == s_win + 1 && best_cost < 1e300) break;
         const uint32_t nrc = nrc_for(range, (uint32_t)s);
-        const double C = std::pow((double)nrc, dims);
+        const double C = tune_cells(nrc, dims);
         if (C > 4.0e9) continue;
         if (s > s_win && C > std::max(4096.0, 64.0 * (double)n)) continue;  // widened: grids in proportion to n
         double E = 0, cmax = 0;
@@ -188,14 +186,8 @@ static TuneResult tune_impl(const uint32_t* boxes, const std::vector<uint64_t>& 
         if (cmax >= (double)(1u << 26)) continue;     // a sampled box would not fit (2^26 cells or more)
         const double Es = E;
         E *= scale;
-        double T;
-        if (exact_tests) {
-            T = tests_in_sample(boxes, idx, dims, (uint32_t)s, nrc, (uint64_t)Es, keys, cnts) * scale * scale;
-        } else {
-            T = E * E / (2.0 * C);
-        }
-        const double occ = 2.0 * T / std::max(E, 1.0) + 1.0;
-        const double cost = kCell * C + kEntry * E + kTest * std::max(1.0, occ / kOccTest) * T;
+        const double T = tests_in_sample(boxes, idx, dims, (uint32_t)s, nrc, (uint64_t)Es, keys, cnts) * scale * scale;
+        const double cost = tune_cost(C, E, T);
         if (cost < best_cost) {
             best_cost = cost;
             best = TuneResult{(uint32_t)s, E, T, C};
@@ -205,7 +197,7 @@ static TuneResult tune_impl(const uint32_t* boxes, const std::vector<uint64_t>& 
         uint32_t s = 31;
         while (s > 0 && nrc_for(range, s - 1) <= 1) s--;
         best.shift = s;
-        best.est_cells = std::pow((double)nrc_for(range, s), dims);
+        best.est_cells = tune_cells(nrc_for(range, s), dims);
         best.est_entries = (double)n;
         best.est_tests = (double)n * n / 2;
     }
@@ -219,14 +211,9 @@ TuneResult tune_shift_sample(const uint32_t* boxes, uint64_t n_avail, uint64_t n
     const uint64_t m = std::min<uint64_t>(n_avail, std::max<uint64_t>(1, max_sample));
     idx.reserve(m);
     for (uint64_t i = 0; i < m; i++) idx.push_back((uint64_t)((unsigned __int128)i * n_avail / m));
-    return tune_impl(boxes, idx, n_true, dims, range, true);
+    return tune_impl(boxes, idx, n_true, dims, range);
 }
 
-TuneResult tune_shift_analytic(const uint32_t* sample, uint64_t nsample, uint64_t n, int dims, uint32_t range) {
-    std::vector<uint64_t> idx(nsample);
-    for (uint64_t i = 0; i < nsample; i++) idx[i] = i;
-    return tune_impl(sample, idx, n, dims, range, false);
-}
 
 // --------------------------------------------------------------------------
 // pipeline
@@ -791,7 +778,7 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_entries,
                       &c->d_lists, &c->d_tasks, &c->d_state,
                       &c->d_out, &c->d_out2, &c->d_ctr, &c->d_scenes, &c->d_scene_off, &c->d_scene_pair,
-                      &c->d_scene_cursor, &c->d_dims, &c->d_scene_tab})
+                      &c->d_scene_cursor, &c->d_dims, &c->d_scene_tab, &c->d_tune})
         b->release();
     c->h_ctr.release();
     c->h_stage.release();
@@ -961,6 +948,7 @@ static int self_or_bip(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const 
         c->stats.grid_retries = tr.shift - first;
     }
     c->up_red = c->up_blue = nullptr;
+    c->scene_shifts.assign(1, tr.shift);
     *npairs = c->npairs;
     return rc;
 }
@@ -996,19 +984,25 @@ PBIG2_API int pbig2_batch_intersect(pbig2_ctx* c, const uint32_t* boxes, const u
     const uint32_t* d_boxes = nullptr;
     int rc = stage_boxes_in(c, boxes, n * W, boxes_loc, st, &d_boxes);
     if (rc) return rc;
-    // per-scene cell size: analytic tuner on a small per-scene sample
+    // per-scene cell sizes: given, or chosen on the device (k_tune_scenes,
+    // one warp per scene on up to 64 of its boxes); one small copy back
     std::vector<GridScene> sc(n_scenes);
     double est_e = 0;
-    const uint64_t kPer = 64;
-    std::vector<uint32_t> smp;
-    if (!cell_shifts && boxes_loc == PBIG2_DEVICE) {
-        // one strided copy per scene would be thousands of calls; sample the
-        // whole batch once and attribute sample boxes to their scenes
-        rc = sample_device_boxes(c, d_boxes, n, (int)dims, std::min<uint64_t>(n, kPer * n_scenes), st, smp);
-        if (rc) return rc;
+    const SceneTune* tuned = nullptr;
+    if (!cell_shifts) {
+        const size_t off_bytes = ((size_t)n_scenes + 1) * 8, tune_bytes = (size_t)n_scenes * sizeof(SceneTune);
+        CK(c->h_stage.ensure(off_bytes + tune_bytes));
+        CK(cudaStreamSynchronize(st));  // staging buffer reuse
+        CK(c->d_tune.ensure(off_bytes + tune_bytes, false, st));
+        memcpy(c->h_stage.p, scene_offsets, off_bytes);
+        const unsigned long long* d_offs = c->d_tune.as<unsigned long long>();
+        SceneTune* d_res = reinterpret_cast<SceneTune*>(c->d_tune.as<char>() + off_bytes);
+        CK(cudaMemcpyAsync(c->d_tune.p, c->h_stage.p, off_bytes, cudaMemcpyHostToDevice, st));
+        CK(launch_tune_scenes(d_boxes, d_offs, n_scenes, (int)dims, range, d_res, st));
+        CK(cudaMemcpyAsync((char*)c->h_stage.p + off_bytes, d_res, tune_bytes, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        tuned = reinterpret_cast<const SceneTune*>((const char*)c->h_stage.p + off_bytes);
     }
-    const uint64_t msmp = smp.size() / W;
-    uint64_t sp = 0;
     for (uint32_t i = 0; i < n_scenes; i++) {
         const uint64_t a = scene_offsets[i], b = scene_offsets[i + 1], ns = b - a;
         uint32_t shift;
@@ -1016,22 +1010,9 @@ PBIG2_API int pbig2_batch_intersect(pbig2_ctx* c, const uint32_t* boxes, const u
         if (cell_shifts) {
             shift = cell_shifts[i];
             if (shift > 31) return fail(PBIG2_EINVAL, "cell_shifts[%u] > 31", i);
-        } else if (boxes_loc == PBIG2_HOST) {
-            const uint64_t m = std::min<uint64_t>(ns, kPer);
-            std::vector<uint32_t> s(m * W);
-            for (uint64_t k = 0; k < m; k++)
-                memcpy(&s[k * W], boxes + (a + (uint64_t)((unsigned __int128)k * ns / m)) * W, W * 4);
-            TuneResult tr = tune_shift_analytic(s.data(), m, ns, (int)dims, range);
-            shift = tr.shift;
-            e = std::max(e, tr.est_entries);
         } else {
-            // sample boxes g*stride that fall inside [a, b)
-            const uint64_t stride = msmp ? n / msmp : 1;
-            const uint64_t s0 = sp;
-            while (sp < msmp && sp * stride < b) sp++;
-            TuneResult tr = tune_shift_analytic(smp.data() + s0 * W, sp - s0, ns, (int)dims, range);
-            shift = tr.shift;
-            e = std::max(e, tr.est_entries);
+            shift = tuned[i].shift;
+            e = std::max(e, tuned[i].est_entries);
         }
         sc[i] = GridScene{a, ns, shift, (int)i};
         est_e += e;
@@ -1052,6 +1033,8 @@ PBIG2_API int pbig2_batch_intersect(pbig2_ctx* c, const uint32_t* boxes, const u
         retries++;
     }
     c->stats.grid_retries = retries;
+    c->scene_shifts.resize(n_scenes);
+    for (uint32_t i = 0; i < n_scenes; i++) c->scene_shifts[i] = sc[i].shift;
     *npairs = c->npairs;
     return rc;
 }
@@ -1203,6 +1186,14 @@ PBIG2_API int pbig2_result_scene_offsets(pbig2_ctx* c, uint64_t* offsets, uint32
     if (c->scene_pair_off.size() != (size_t)n_scenes + 1)
         return fail(PBIG2_EINVAL, "last result has %zu scenes", c->scene_pair_off.size() - 1);
     memcpy(offsets, c->scene_pair_off.data(), (n_scenes + 1) * 8);
+    return PBIG2_OK;
+}
+
+PBIG2_API int pbig2_result_scene_shifts(pbig2_ctx* c, uint32_t* shifts, uint32_t n_scenes) {
+    if (!c || !shifts) return fail(PBIG2_EINVAL, "bad arguments");
+    if (c->scene_shifts.size() != (size_t)n_scenes)
+        return fail(PBIG2_EINVAL, "last query has %zu scenes", c->scene_shifts.size());
+    memcpy(shifts, c->scene_shifts.data(), (size_t)n_scenes * 4);
     return PBIG2_OK;
 }
 

@@ -40,7 +40,6 @@ struct TuneResult {
 };
 TuneResult tune_shift_sample(const uint32_t* boxes, uint64_t n_avail, uint64_t n_true, int dims, uint32_t range,
                              uint64_t max_sample);
-TuneResult tune_shift_analytic(const uint32_t* sample, uint64_t nsample, uint64_t n, int dims, uint32_t range);
 uint32_t nrc_for(uint32_t range, uint32_t shift);
 // records `msg` as the calling thread's pbig2_last_error() and returns code
 int api_fail(int code, const char* msg);
@@ -62,7 +61,7 @@ struct pbig2_ctx {
     uint32_t merged_blocks = 0;  // merged blocks of the last query
     uint32_t last_err = 0;       // error bits of the last pipeline pass
     pbig::DevBuf d_boxes, d_counts, d_entries, d_lists, d_tasks, d_state, d_out, d_out2, d_ctr,
-        d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims, d_scene_tab;
+        d_scenes, d_scene_off, d_scene_pair, d_scene_cursor, d_dims, d_scene_tab, d_tune;
     pbig::HostPinned h_ctr, h_stage;
     // caller's pair buffer for self/bipartite queries (pbig2_set_pair_output)
     uint2* ext_out = nullptr;
@@ -83,6 +82,7 @@ struct pbig2_ctx {
     const uint2* result = nullptr;
     uint64_t npairs = 0;
     std::vector<uint64_t> scene_pair_off;
+    std::vector<uint32_t> scene_shifts;  // cell-size shift of every scene of the last query
     pbig2_stats stats{};
     // capacity hints carried between queries
     uint64_t out_hint = 0;

@@ -88,6 +88,101 @@ __global__ void k_scene_table(Params pin) {
 }
 
 // ---------------------------------------------------------------------------
+// per-scene cell sizes of a batched query: one warp per scene runs the host
+// tuner's analytic model (tune_impl with T = E^2 / 2C) on the rows
+// a + floor(k * n / m), k < m = min(n, 64), of the scene [a, a + n). Every
+// sum is of integers (exact in any order), so the choice equals the host
+// model's on the same rows.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kTuneRows = 64;
+
+__device__ __forceinline__ uint32_t nrc_dev(uint32_t range, int s) {
+    return (uint32_t)(((uint64_t)range + (1ull << s) - 1) >> s);
+}
+
+__global__ void k_tune_scenes(const uint32_t* boxes, const unsigned long long* offs, uint32_t nsc, int dims,
+                              uint32_t range, SceneTune* out) {
+    const uint32_t lane = lane_id();
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t W = 2 * (uint32_t)dims + 1;
+    for (uint64_t sc = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; sc < nsc; sc += nw) {
+        const uint64_t a = offs[sc];
+        const uint64_t n = offs[sc + 1] > a ? offs[sc + 1] - a : 0;
+        const uint64_t m = n < kTuneRows ? n : kTuneRows;
+        uint32_t lo[2][3] = {{0, 0, 0}, {0, 0, 0}}, hi[2][3] = {{0, 0, 0}, {0, 0, 0}};
+        bool ok[2] = {false, false};
+        uint64_t ext = 0, good = 0;
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const uint64_t k = lane + 32u * j;
+            if (k >= m) continue;
+            const uint32_t* b = boxes + (a + k * n / m) * W;
+            bool v = true;
+            for (int d = 0; d < dims; d++) {
+                lo[j][d] = b[2 * d];
+                hi[j][d] = b[2 * d + 1];
+                v = v && lo[j][d] <= hi[j][d] && hi[j][d] < range;
+            }
+            ok[j] = v;
+            if (v) {
+                for (int d = 0; d < dims; d++) ext += (uint64_t)(hi[j][d] - lo[j][d]) + 1;
+                good++;
+            }
+        }
+        ext = warp_sum_u64(ext);
+        good = warp_sum_u64(good);
+        SceneTune best{0u, 0u, 0.0};
+        if (m == 0) {
+            uint32_t s = 31;
+            while (s > 0 && nrc_dev(range, (int)s - 1) <= 1) s--;
+            best.shift = s;
+        } else {
+            const int s0 = tune_s0(ext, (good ? good : 1) * (uint64_t)dims);
+            const double scale = (double)n / (double)m;
+            const int s_win = s0 + 3 < 31 ? s0 + 3 : 31;
+            double best_cost = 1e300;
+            for (int s = s0 - 2 > 0 ? s0 - 2 : 0; s <= 31; s++) {
+                if (s == s_win + 1 && best_cost < 1e300) break;
+                const double C = tune_cells(nrc_dev(range, s), dims);
+                if (C > 4.0e9) continue;
+                if (s > s_win && C > fmax(4096.0, 64.0 * (double)n)) continue;
+                double e = 0, cm = 0;
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    if (!ok[j]) continue;
+                    double c = 1;
+                    for (int d = 0; d < dims; d++) c = tune_mul(c, (double)((hi[j][d] >> s) - (lo[j][d] >> s) + 1));
+                    e = tune_add(e, c);
+                    cm = fmax(cm, c);
+                }
+#pragma unroll
+                for (int o = 16; o; o >>= 1) {
+                    e = tune_add(e, __shfl_xor_sync(FULL_MASK, e, o));
+                    cm = fmax(cm, __shfl_xor_sync(FULL_MASK, cm, o));
+                }
+                if (e / (double)m > 64.0) continue;
+                if (cm >= (double)(1u << 26)) continue;
+                const double E = tune_mul(e, scale);
+                const double T = tune_mul(E, E) / tune_mul(2.0, C);
+                const double cost = tune_cost(C, E, T);
+                if (cost < best_cost) {
+                    best_cost = cost;
+                    best.shift = (uint32_t)s;
+                    best.est_entries = E;
+                }
+            }
+            if (best_cost == 1e300) {  // the coarsest grid that is not a single cell
+                uint32_t s = 31;
+                while (s > 0 && nrc_dev(range, (int)s - 1) <= 1) s--;
+                best.shift = s;
+                best.est_entries = (double)n;
+            }
+        }
+        if (lane == 0) out[sc] = best;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // count / scatter: one thread per box, boxes staged through shared memory with
 // 16-byte vector loads; the cells of the 32 boxes of a warp are enumerated
 // cooperatively (lane q handles cell q of the warp's concatenated cell list),
@@ -1833,6 +1928,15 @@ cudaError_t launch_scene_offsets(const Params& p, const unsigned long long* hist
                                  uint32_t nscenes_cap, cudaStream_t st) {
     (void)nscenes_cap;
     k_scene_offsets<<<1, 1024, 0, st>>>(p, hist, off);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tune_scenes(const uint32_t* boxes, const unsigned long long* offs, uint32_t nscenes, int dims,
+                               uint32_t range, SceneTune* out, cudaStream_t st) {
+    if (nscenes == 0) return cudaSuccess;
+    const uint64_t blocks = ((uint64_t)nscenes + 7) / 8;  // 8 warps (scenes) per block
+    const uint64_t cap = (uint64_t)(g_sm_count > 0 ? g_sm_count : 152) * 16;
+    k_tune_scenes<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, st>>>(boxes, offs, nscenes, dims, range, out);
     return cudaGetLastError();
 }
 

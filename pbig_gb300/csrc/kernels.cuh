@@ -46,6 +46,57 @@ __host__ __device__ inline uint64_t grid_cells(uint32_t range, uint32_t shift, i
     return c;
 }
 
+// Cell-size cost model shared by the host tuner and the per-scene device
+// tuner of batched queries: cost(s) = kCell*C + kEntry*E + kTest*T seconds
+// (C cells, E box-in-cell entries, T pair tests), with kTest scaled by
+// max(1, m / kOccTest) for the entry-weighted mean occupancy m = 2T/E + 1.
+// The products are rounded one at a time (no fused multiply-add), so that
+// host and device compute the same costs.
+constexpr double kTuneCell = 2.4e-12, kTuneEntry = 80.0e-12, kTuneTest = 0.9e-12, kTuneOcc = 96.0;
+
+__host__ __device__ inline double tune_mul(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+__host__ __device__ inline double tune_add(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+__host__ __device__ inline double tune_cost(double C, double E, double T) {
+    const double occ = tune_add(tune_mul(2.0, T) / (E > 1.0 ? E : 1.0), 1.0);
+    const double f = occ / kTuneOcc > 1.0 ? occ / kTuneOcc : 1.0;
+    return tune_add(tune_add(tune_mul(kTuneCell, C), tune_mul(kTuneEntry, E)), tune_mul(tune_mul(kTuneTest, f), T));
+}
+// C = nrc^dims in double (rounded product; exact below 2^53)
+__host__ __device__ inline double tune_cells(uint64_t nrc, int dims) {
+    double c = (double)nrc;
+    for (int d = 1; d < dims; d++) c = tune_mul(c, (double)nrc);
+    return c;
+}
+// floor(log2(mean box extent)), at least 0, from the exact integer sum of
+// the sampled extents (sum of (max - min + 1) over boxes and axes)
+__host__ __device__ inline int tune_s0(uint64_t ext_sum, uint64_t nvals) {
+    const double mean = (double)ext_sum / (double)(nvals ? nvals : 1);
+    if (!(mean >= 2.0)) return 0;
+    const uint64_t f = (uint64_t)mean;  // floor; log2 of a real >= 1 floors to that of its floor
+    int k = 0;
+    while ((f >> (k + 1)) != 0) k++;
+    return k;
+}
+
+// result of the per-scene device tuner (batched queries)
+struct SceneTune {
+    uint32_t shift;
+    uint32_t pad;
+    double est_entries;
+};
+
 struct Scene {
     uint32_t box_off;   // first box of the scene (global index)
     uint32_t n;         // boxes in the scene
@@ -128,6 +179,11 @@ cudaError_t launch_scan(const Params& p, cudaStream_t st);
 cudaError_t launch_expand(const Params& p, cudaStream_t st);
 cudaError_t launch_scatter(const Params& p, int dims, cudaStream_t st);
 // exclusive scan of nscenes+1 per-scene pair counts (one block)
+// per-scene cell sizes of a batched query (one warp per scene, a strided
+// sample of up to 64 boxes of each scene, T estimated as E^2 / 2C); offs:
+// nscenes+1 box offsets in device memory
+cudaError_t launch_tune_scenes(const uint32_t* boxes, const unsigned long long* offs, uint32_t nscenes, int dims,
+                               uint32_t range, SceneTune* out, cudaStream_t st);
 cudaError_t launch_scene_offsets(const Params& p, const unsigned long long* hist, unsigned long long* off,
                                  uint32_t nscenes_cap, cudaStream_t st);
 // Pairs bound for page-locked host memory are limited by the host link, not

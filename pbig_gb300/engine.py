@@ -32,7 +32,7 @@ EXPORTS = [
     "pbig2_noalloc_last_error", "pbig2_set_option", "pbig2_scene_create", "pbig2_scene_destroy",
     "pbig2_scene_move", "pbig2_scene_delta", "pbig2_scene_pairs", "pbig2_scene_boxes", "pbig2_scene_copy",
     "pbig2_result_records", "pbig2_copy_records", "pbig2_decode_records", "pbig2_serve_batch",
-    "pbig2_grid_cells",
+    "pbig2_grid_cells", "pbig2_result_scene_shifts",
 ]
 
 
@@ -96,6 +96,7 @@ def lib():
         L.pbig2_copy_records.argtypes = [vp, vp, vp, vp]
         L.pbig2_decode_records.argtypes = [vp, u64, vp, u64, vp, u64, vp, u64, C.POINTER(u64)]
         L.pbig2_result_scene_offsets.argtypes = [vp, C.POINTER(u64), u32]
+        L.pbig2_result_scene_shifts.argtypes = [vp, C.POINTER(u32), u32]
         L.pbig2_get_stats.argtypes = [vp, C.POINTER(Stats)]
         L.pbig2_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
         L.pbig2_host_free.argtypes = [vp]
@@ -153,6 +154,7 @@ class Engine:
         self.last_rc = OK
         self._keep = None
         self._out = None
+        self._nscenes = 1
 
     def close(self):
         if getattr(self, "_ctx", None):
@@ -187,6 +189,7 @@ class Engine:
                                           AUTO if cell_shift is None else cell_shift, loc,
                                           self._stream(stream), C.byref(out))
         self.last_rc = _check(rc, (OK, EINPUT) if allow_bad else (OK,))
+        self._nscenes = 1
         return out.value
 
     def bipartite_intersect(self, red, blue, range_: int, cell_shift: int | None = None, stream=None) -> int:
@@ -201,6 +204,7 @@ class Engine:
                                                AUTO if cell_shift is None else cell_shift, lr,
                                                self._stream(stream), C.byref(out))
         self.last_rc = _check(rc)
+        self._nscenes = 1
         return out.value
 
     def batch_intersect(self, boxes, scene_offsets, range_: int, cell_shifts=None, stream=None) -> int:
@@ -245,6 +249,14 @@ class Engine:
         ns = self._nscenes
         out = np.empty(ns + 1, dtype=np.uint64)
         _check(self._L.pbig2_result_scene_offsets(self._ctx, out.ctypes.data_as(C.POINTER(C.c_uint64)), ns))
+        return out
+
+    def scene_shifts(self, n_scenes: int | None = None) -> np.ndarray:
+        """Cell size (log2) of every scene of the last query (1 for a self or
+        red/blue query)."""
+        ns = self._nscenes if n_scenes is None else n_scenes
+        out = np.empty(ns, dtype=np.uint32)
+        _check(self._L.pbig2_result_scene_shifts(self._ctx, out.ctypes.data_as(C.POINTER(C.c_uint32)), ns))
         return out
 
     def pairs(self, first: int = 0, count: int | None = None) -> np.ndarray:

@@ -1,6 +1,7 @@
 """The batched workload at full size: 4,096 independent 3-D scenes of
 log-uniform sizes in [256, 262,144] boxes (1.54e8 boxes in all), every
-scene's cell size chosen inside the call. Each scene's pair list must equal
+scene's cell size chosen inside the call by the device tuner (its choices
+must equal a restatement of the cost model). Each scene's pair list must equal
 the plain single-scene path's list (all 4,096 scenes, compared on the device
 after sorting) and the oracle's (a stratified sample: the 20 largest scenes
 and every 128th scene in size order).
@@ -14,6 +15,7 @@ import pytest
 
 from oracle import oracle as O
 from pbig_gb300 import Engine, gen
+from test_tuner import analytic_shift
 
 pytestmark = pytest.mark.gpu
 
@@ -37,6 +39,10 @@ def test_full_batched_workload_scene_by_scene():
         e.pairs_into(res)
         e.sync()
         assert e.stats()["bad_boxes"] == 0
+        # the device tuner's choice for every scene equals the cost model's
+        shifts = e.scene_shifts()
+        want_shifts = [analytic_shift(boxes[int(offs[i]):int(offs[i + 1])], gen.RANGE) for i in range(4096)]
+        assert np.array_equal(shifts, np.array(want_shifts, dtype=np.uint32))
         # every scene against the plain path
         bad = []
         for i in range(4096):

@@ -85,3 +85,60 @@ def test_sampled_boxes_always_fit(seed):
     assert 0 <= s <= 31
     assert box_cells(b, s).max() < 1 << 26
     assert grid_cells(rng, s, dims) < 1 << 32
+
+
+def analytic_shift(b, rng):
+    """Restatement of the per-scene tuner of batched queries (the engine's
+    cost model with T = E^2 / 2C on the rows floor(k * n / m), k < m =
+    min(n, 64)), in the same double arithmetic."""
+    n = b.shape[0]
+    dims = (b.shape[1] - 1) // 2
+
+    def nrc(s):
+        return (rng + (1 << s) - 1) >> s
+
+    def coarsest():
+        s = 31
+        while s > 0 and nrc(s - 1) <= 1:
+            s -= 1
+        return s
+
+    if n == 0:
+        return coarsest()
+    m = min(n, 64)
+    smp = b[[k * n // m for k in range(m)]].astype(np.int64)
+    lo, hi = smp[:, 0:2 * dims:2], smp[:, 1:2 * dims:2]
+    ok = ((lo <= hi) & (hi < rng)).all(axis=1)
+    ext, good = int((hi - lo + 1)[ok].sum()), int(ok.sum())
+    mean = ext / ((good if good else 1) * dims)
+    s0 = int(mean).bit_length() - 1 if mean >= 2.0 else 0
+    scale = n / m
+    s_win = min(31, s0 + 3)
+    best, best_s = 1e300, None
+    for s in range(max(0, s0 - 2), 32):
+        if s == s_win + 1 and best < 1e300:
+            break
+        C = float(nrc(s))
+        for _ in range(1, dims):
+            C = C * float(nrc(s))
+        if C > 4.0e9:
+            continue
+        if s > s_win and C > max(4096.0, 64.0 * n):
+            continue
+        E, cmax = 0.0, 0.0
+        for i in np.nonzero(ok)[0]:
+            c = 1.0
+            for d in range(dims):
+                c = c * float((int(hi[i, d]) >> s) - (int(lo[i, d]) >> s) + 1)
+            E += c
+            cmax = max(cmax, c)
+        if E / m > 64.0 or cmax >= float(1 << 26):
+            continue
+        E = E * scale
+        T = E * E / (2.0 * C)
+        occ = 2.0 * T / max(E, 1.0) + 1.0
+        f = occ / 96.0 if occ / 96.0 > 1.0 else 1.0
+        cost = (2.4e-12 * C + 80.0e-12 * E) + (0.9e-12 * f) * T
+        if cost < best:
+            best, best_s = cost, s
+    return coarsest() if best_s is None else best_s
