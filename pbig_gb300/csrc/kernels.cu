@@ -1281,17 +1281,66 @@ __device__ __forceinline__ uint32_t miss_word(const Box& a, const uint4& ca, con
 
 __device__ __forceinline__ uint32_t push_hit(uint32_t mask, uint32_t miss) { return __funnelshift_l(~miss, mask, 1); }
 
-template <int D, bool NARROW>
-__device__ __forceinline__ uint32_t test_slot(const Slots& s, const Box& me, uint32_t mask, uint32_t i) {
+// Medium-cell staging. With coordinates < 2^29 a slot holds its box as the
+// six signed terms (-x1, x0, -y1, y0, -z1, z0) (then f and the index), and a
+// row box is taken as the partner terms (x0-1, -x1-1, y0-1, -y1-1, z0-1,
+// -z1-1). Each sum row_k + col_k is the gap between the two boxes along one
+// axis and side minus one (a.x0 - c.x1 - 1, c.x0 - a.x1 - 1, ...), so the
+// closed boxes overlap iff the largest of the six sums is negative: one add
+// and five add-max instructions per test, the result's sign bit the hit.
+// Wider coordinates keep the plain layout and comparisons.
+struct SepRow {
+    int t0, t1, t2, t3, t4, t5;
+};
+template <bool NARROW> struct MedRowT { using type = Box; };
+template <> struct MedRowT<true> { using type = SepRow; };
+
+template <bool NARROW>
+__device__ __forceinline__ void med_slot_put(const Slots& s, uint32_t i, const Box& x) {
+    if constexpr (NARROW) {
+        s.a[i] = make_uint4(0u - x.x1, x.x0, 0u - x.y1, x.y0);
+        s.b[i] = make_uint4(0u - x.z1, x.z0, x.f, x.id);
+    } else {
+        slot_put(s, i, x);
+    }
+}
+
+// the row form of a staged box (st: slot_get of its slot)
+template <bool NARROW>
+__device__ __forceinline__ typename MedRowT<NARROW>::type med_row(const Box& st) {
+    if constexpr (NARROW) {  // slot_get maps (-x1, x0, -y1, y0, -z1, z0) to (x0, x1, y0, y1, z0, z1)
+        return SepRow{(int)st.x1 - 1, (int)st.x0 - 1, (int)st.y1 - 1, (int)st.y0 - 1, (int)st.z1 - 1, (int)st.z0 - 1};
+    } else {
+        return st;
+    }
+}
+
+// bit 31 set iff row box r and column box (ca, cz) overlap
+template <int D>
+__device__ __forceinline__ uint32_t sep_hit(const SepRow& r, const uint4& ca, const uint2& cz) {
+    int m = r.t0 + (int)ca.x;
+    m = __viaddmax_s32(r.t1, (int)ca.y, m);
+    m = __viaddmax_s32(r.t2, (int)ca.z, m);
+    m = __viaddmax_s32(r.t3, (int)ca.w, m);
+    if (D == 3) {
+        m = __viaddmax_s32(r.t4, (int)cz.x, m);
+        m = __viaddmax_s32(r.t5, (int)cz.y, m);
+    }
+    return (uint32_t)m;
+}
+
+template <int D, bool NARROW, class Row>
+__device__ __forceinline__ uint32_t test_slot(const Slots& s, const Row& me, uint32_t mask, uint32_t i) {
     const uint4 ca = s.a[i];
     const uint2 cz = D == 3 ? *reinterpret_cast<const uint2*>(&s.b[i]) : make_uint2(0u, 0u);
-    return push_hit(mask, miss_word<D, NARROW>(me, ca, cz));
+    if constexpr (NARROW) return __funnelshift_l(sep_hit<D>(me, ca, cz), mask, 1);
+    else return push_hit(mask, miss_word<D, false>(me, ca, cz));
 }
 
 // row box against columns [c0, c0 + cnt), cnt a multiple of 8 up to 32;
 // bit cnt-1-j of the result: column j
-template <int D, bool NARROW>
-__device__ __forceinline__ uint32_t sweep_tile(const Slots& s, const Box& me, uint32_t c0, uint32_t cnt) {
+template <int D, bool NARROW, class Row>
+__device__ __forceinline__ uint32_t sweep_tile(const Slots& s, const Row& me, uint32_t c0, uint32_t cnt) {
     uint32_t mask = 0;
     if (cnt == 32) {
 #pragma unroll
@@ -1309,8 +1358,8 @@ __device__ __forceinline__ uint32_t sweep_tile(const Slots& s, const Box& me, ui
 // partners l+1 .. l+floor(m/2) (mod m), lanes past m/2 one fewer when m is
 // even (the BALANCE=1 sweep of d_matching, pbig.cu:804-825), so each
 // unordered pair is tested once; bit dmax-d of the result: partner l+d
-template <int D, bool NARROW>
-__device__ __forceinline__ uint32_t sweep_diag2(const Slots& s, const Box& me, uint32_t l, uint32_t rb, uint32_t m) {
+template <int D, bool NARROW, class Row>
+__device__ __forceinline__ uint32_t sweep_diag2(const Slots& s, const Row& me, uint32_t l, uint32_t rb, uint32_t m) {
     uint32_t mask = 0;
     if (m == 32) {
 #pragma unroll
@@ -1368,14 +1417,15 @@ __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
 #pragma unroll
         for (uint32_t k = 0; k < kMedSlots / 32; k++) {
             const uint32_t e = lane + 32 * k;
-            if (e < 32 * R) slot_put(s, e, e < n ? load_box<D, NARROW>(p, raw[k]) : dummy_box<NARROW>());
+            if (e < 32 * R) med_slot_put<NARROW>(s, e, e < n ? load_box<D, NARROW>(p, raw[k]) : dummy_box<NARROW>());
         }
         __syncwarp();
         for (uint32_t r = 0; r < R; r++) {
             const uint32_t rows = min(32u, n - 32 * r), rb = 32 * r;
             const Box me = slot_get(s, rb + lane);  // lanes >= rows hold a padding box, masked below
+            const auto row = med_row<NARROW>(me);
             const uint32_t l = lane < rows ? lane : 0u;
-            const uint32_t dm = sweep_diag2<D, NARROW>(s, me, l, rb, rows) &
+            const uint32_t dm = sweep_diag2<D, NARROW>(s, row, l, rb, rows) &
                                 diag_allow(tile_allow<BIP>(p, s, rb, rows, me), lane, rows);
             const uint32_t dmax = rows >> 1;
             auto pdiag = [&](uint32_t k) {
@@ -1392,7 +1442,7 @@ __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
                 uint32_t mc = 0;
                 const uint32_t cnt = (ncol + 7) & ~7u;
                 if (__any_sync(FULL_MASK, allow != 0u))
-                    mc = sweep_tile<D, NARROW>(s, me, c0, cnt) & (__brev(allow) >> (32u - cnt));
+                    mc = sweep_tile<D, NARROW>(s, row, c0, cnt) & (__brev(allow) >> (32u - cnt));
                 auto pcol = [&](uint32_t k) { return slot_id(s, c0 + cnt - 1 - k); };
                 if constexpr (REC) {
                     auto lcol = [&](uint32_t k) { return c0 + cnt - 1 - k; };
