@@ -215,6 +215,16 @@ PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
  * kernel on the rest, so the link is not idle while they compute. A
  * negative value runs the three kernels one after another. */
 #define PBIG2_OPT_HOST_SPLIT 4
+/* PBIG2_OPT_ONE_LAUNCH (default 1): a self query of at most 262 144 boxes
+   with an automatic cell size (or a given one whose grid has at most 2^20
+   cells), outside merged and record mode, runs as one cooperative kernel
+   launch: cell size, count, scan, scatter and pair test, separated by grid
+   barriers. A result that does not fit the buffers the launch was given is
+   redone by the regular pipeline. 0 sends every query to the regular
+   pipeline. The value 2 tests the barriers' bounded wait: in the next
+   one-launch query no barrier completes, every block gives up after about a
+   second and the query returns PBIG2_ETIMEOUT; later queries run normally. */
+#define PBIG2_OPT_ONE_LAUNCH 5
 PBIG2_API int pbig2_set_option(pbig2_ctx* ctx, int option, int64_t value);
 
 /* One batch of the serving loop (no counterpart in the reference; the

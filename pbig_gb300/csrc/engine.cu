@@ -316,7 +316,8 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
 
 // result bookkeeping after a pass: pair count, per-scene offsets, stats
 static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t ncells, uint32_t nsc,
-                        const std::vector<GridScene>& scenes, bool grouped, int launches, cudaStream_t st) {
+                        const std::vector<GridScene>& scenes, bool grouped, int launches, cudaStream_t st,
+                        bool phases = true) {
     c->result_records = c->rice_mode && !grouped;
     c->rice_words = c->result_records ? h.pairs : 0;
     c->npairs = c->result_records ? h.rec_pairs : h.pairs;
@@ -333,13 +334,13 @@ static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t nc
         c->scene_pair_off.push_back(c->npairs);
     }
     float ms = 0;
-    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    if (phases) cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     double phase[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < 5; k++) {
+    for (int k = 0; k < 5 && phases; k++) {
         float x = 0;
         if (cudaEventElapsedTime(&x, c->evp[k], c->evp[k + 1]) == cudaSuccess) phase[k] = x;
     }
-    {
+    if (phases) {
         float x = 0;
         if (grouped && cudaEventElapsedTime(&x, c->evp[5], c->ev1) == cudaSuccess) phase[5] = x;
         // (the pair kernels may overlap: a phase that ends before the
@@ -485,6 +486,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
                         cudaStream_t st, bool group) {
     const uint32_t nsc = (uint32_t)scenes.size();
     c->last_err = 0;
+    c->fused_dirty = true;  // this pipeline leaves cell starts in the counters
     if (nboxes > (uint64_t)kIdMask + 1)
         return fail(PBIG2_EINVAL, "a query holds at most 2^29 boxes (got %llu)", (unsigned long long)nboxes);
     // scene table
@@ -693,6 +695,106 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     return rc;
 }
 
+// One-launch query of a small scene (kernels.cuh: launch_fused). Returns
+// kFusedRedo when the result did not fit the buffers it was given (the
+// caller then runs the regular pipeline, and the hints grow for next time).
+constexpr int kFusedRedo = -1000;
+
+static bool fused_eligible(const pbig2_ctx* c, uint64_t n, int dims, uint32_t range, uint32_t cell_shift) {
+    if (!c->use_fused || fused_blocks() <= 0 || c->merged_mode || c->rice_mode) return false;
+    if (n == 0 || n > kFusedMaxBoxes) return false;
+    return cell_shift == PBIG2_AUTO || grid_cells(range, cell_shift, dims) <= kFusedMaxCells;
+}
+
+static int fused_query(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t n, int dims, uint32_t range,
+                       uint32_t cell_shift, cudaStream_t st) {
+    c->last_err = 0;
+    const uint64_t cells_cap = cell_shift == PBIG2_AUTO ? kFusedMaxCells : grid_cells(range, cell_shift, dims);
+    void* counts_before = c->d_counts.p;
+    CK(c->d_counts.ensure(cells_cap * 4 + 16, false, st));
+    if (c->d_counts.p != counts_before) c->fused_dirty = true;
+    CK(c->d_state.ensure(kFusedMaxCells / 512 * 4 + 8192 * 4, false, st));  // chunk totals, then small-grid cell ends
+    CK(c->h_ctr.ensure(sizeof(Ctr)));
+    CK(c->d_scenes.ensure(sizeof(Scene), false, st));
+    if (!c->d_bar.p || !c->d_fctr.p) {
+        CK(c->d_bar.ensure(sizeof(unsigned int), true, st));
+        CK(c->d_fctr.ensure(2 * sizeof(Ctr), true, st));
+        c->bar_base = 0;
+        c->fused_slot = 0;
+    }
+    const uint64_t entry_cap = std::max<uint64_t>({c->fused_entry_hint, 8 * n + 4096, c->d_entries.bytes / 4});
+    const uint64_t out_cap = std::max<uint64_t>({c->out_hint, n * 4, 1u << 16, c->d_out.bytes / 8});
+    const uint64_t task_cap = std::max<uint64_t>(c->d_tasks.bytes / 16, 4096);
+    const bool use_ext = c->ext_out != nullptr;
+    Ctr* slots = c->d_fctr.as<Ctr>();
+    Params p{};
+    p.boxes = d_boxes;
+    p.nboxes = n;
+    p.scenes = c->d_scenes.as<Scene>();
+    p.nscenes = 1;
+    p.split = kNoSplit;
+    p.max_range = range;
+    p.tile_state = c->d_state.as<unsigned long long>();
+    int rc = ensure_query_buffers(c, p, entry_cap, use_ext ? 1 : out_cap, task_cap, 1, false, st);
+    if (rc) return rc;
+    p.ctr = slots + c->fused_slot;
+    if (use_ext) {
+        p.out = c->ext_out;
+        p.out_cap = c->ext_cap;
+    }
+    FusedArgs a{};
+    a.bar = c->d_bar.as<unsigned int>();
+    // (test of the bounded wait: a count far ahead of every arrival)
+    a.bar_base = c->fused_stall_test ? c->bar_base + (1u << 24) : c->bar_base;
+    c->fused_stall_test = false;
+    a.chunk_sum = c->d_state.as<uint32_t>();
+    a.ends = c->d_state.as<uint32_t>() + kFusedMaxCells / 512;
+    a.scenes = c->d_scenes.as<Scene>();
+    a.ctr_next = slots + (c->fused_slot ^ 1);
+    a.zero_cells = c->fused_dirty ? std::min<uint64_t>(kFusedMaxCells, c->d_counts.bytes / 4) : 0;
+    a.shift = cell_shift == PBIG2_AUTO ? kFusedTune : cell_shift;
+    // the kernel's last block writes the counters to h_ctr (page-locked);
+    // `barriers` stays at this mark when the launch gave up before that
+    Ctr* hc = static_cast<Ctr*>(c->h_ctr.p);
+    hc->barriers = 0xffffffffu;
+    a.ctr_host = hc;
+    CK(launch_fused(p, a, dims, st));
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(PBIG2_ECUDA, "one-launch query failed: %s", cudaGetErrorString(e));
+    Ctr h{};
+    memcpy(&h, hc, sizeof(Ctr));
+    if (h.barriers == 0xffffffffu) {  // no block copied the counters: read them
+        CK(cudaMemcpy(&h, p.ctr, sizeof(Ctr), cudaMemcpyDeviceToHost));
+        h.err |= kErrWait;
+    }
+    if (h.err & kErrWait) {
+        // the barriers' count and the counters are unknown now: start again from zero
+        CK(cudaMemsetAsync(c->d_bar.p, 0, sizeof(unsigned int), st));
+        CK(cudaMemsetAsync(c->d_fctr.p, 0, 2 * sizeof(Ctr), st));
+        CK(cudaStreamSynchronize(st));
+        c->bar_base = 0;
+        c->fused_slot = 0;
+        c->fused_dirty = true;
+        return fail(PBIG2_ETIMEOUT, "a bounded device wait gave up (grid barrier of a one-launch query)");
+    }
+    c->bar_base += h.barriers * (unsigned int)fused_blocks();
+    c->fused_slot ^= 1;
+    c->fused_dirty = false;
+    if (h.err & kErrIndex) return fail(PBIG2_ECUDA, "inconsistent cell lists (error bits 0x%x)", h.err);
+    if ((h.err & (kErrEntryOvf | kErrTaskOvf | kErrOutOvf)) || h.entries > p.entry_cap || h.pairs > p.out_cap) {
+        c->fused_entry_hint = std::max<uint64_t>(c->fused_entry_hint, h.entries + h.entries / 8 + 4096);
+        if (!use_ext || h.pairs <= p.out_cap) c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
+        return kFusedRedo;
+    }
+    c->result_ext = use_ext;
+    c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
+    c->merged_blocks = 0;
+    std::vector<GridScene> sc{{0, n, h.shift, 0}};
+    rc = finish_query(c, h, n, h.cells, 1, sc, false, 1, st, false);
+    c->stats.device_ms = h.t_end > h.t_start ? (double)(h.t_end - h.t_start) * 1e-6 : 0.0;  // the kernel's own clock
+    return rc;
+}
+
 static cudaStream_t pick_stream(pbig2_ctx* c, void* stream) {
     return stream ? (cudaStream_t)stream : c->own_stream;
 }
@@ -775,7 +877,7 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     cudaSetDevice(c->device);
     if (c->own_stream) cudaStreamSynchronize(c->own_stream);
     c->drop_graph();
-    for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_entries,
+    for (DevBuf* b : {&c->d_boxes, &c->d_counts, &c->d_entries, &c->d_bar, &c->d_fctr,
                       &c->d_lists, &c->d_tasks, &c->d_state,
                       &c->d_out, &c->d_out2, &c->d_ctr, &c->d_scenes, &c->d_scene_off, &c->d_scene_pair,
                       &c->d_scene_cursor, &c->d_dims, &c->d_scene_tab, &c->d_tune})
@@ -872,6 +974,16 @@ static int self_or_bip(pbig2_ctx* c, const uint32_t* red, uint64_t n_red, const 
     const bool bip = blue != nullptr;
     const uint64_t n = n_red + n_blue;
     const uint32_t* d_boxes = nullptr;
+    if (!bip && fused_eligible(c, n, (int)dims, range, cell_shift)) {
+        int rc = stage_boxes_in(c, red, n * W, loc, st, &d_boxes);
+        if (rc) return rc;
+        rc = fused_query(c, d_boxes, n, (int)dims, range, cell_shift, st);
+        if (rc != kFusedRedo) {
+            c->scene_shifts.assign(1, c->stats.cell_shift);
+            *npairs = c->npairs;
+            return rc;
+        }
+    }
     // page-locked host input needs no copy before the pipeline: the count
     // kernel reads it over the host link and writes the device copy
     const uint32_t* m_red = loc == PBIG2_HOST && n_red ? mapped_host(red) : nullptr;
@@ -1210,6 +1322,14 @@ PBIG2_API int pbig2_set_option(pbig2_ctx* c, int option, int64_t value) {
     }
     if (option == PBIG2_OPT_RICE) {
         c->rice_mode = value != 0;
+        return PBIG2_OK;
+    }
+    if (option == PBIG2_OPT_ONE_LAUNCH) {
+        if (value == 2) {  // test of the bounded wait: the next launch's barriers never complete
+            c->fused_stall_test = true;
+            return PBIG2_OK;
+        }
+        c->use_fused = value != 0;
         return PBIG2_OK;
     }
     if (option == PBIG2_OPT_HOST_SPLIT) {

@@ -109,6 +109,16 @@ struct pbig2_ctx {
         if (graph.exec) cudaGraphExecDestroy(graph.exec);
         graph = Graph();
     }
+    // one-launch queries of small scenes (PBIG2_OPT_ONE_LAUNCH): the grid
+    // barriers' arrival counter and its value before the next launch, and
+    // the entry capacity the last one needed
+    bool use_fused = true;
+    pbig::DevBuf d_bar, d_fctr;  // barrier arrivals; two slots of run counters (a launch zeroes the other)
+    unsigned int bar_base = 0;
+    int fused_slot = 0;
+    bool fused_dirty = true;     // the counters may hold values another pipeline left (or are new)
+    uint64_t fused_entry_hint = 0;
+    bool fused_stall_test = false;  // the next launch's barriers never complete (test of the bounded wait)
     // autotuner memo: (n, dims, range, mean extent) -> shift
     struct TuneMemo { uint64_t n; int dims; uint32_t range; double ext; uint32_t shift; double est_e; };
     std::vector<TuneMemo> memo;

@@ -100,14 +100,13 @@ __device__ __forceinline__ uint32_t nrc_dev(uint32_t range, int s) {
     return (uint32_t)(((uint64_t)range + (1ull << s) - 1) >> s);
 }
 
-__global__ void k_tune_scenes(const uint32_t* boxes, const unsigned long long* offs, uint32_t nsc, int dims,
-                              uint32_t range, SceneTune* out) {
+// one warp: the cell shift of the scene of n boxes at row a (grids of at
+// most max_cells cells)
+__device__ __forceinline__ SceneTune tune_scene_warp(const uint32_t* boxes, uint64_t a, uint64_t n, int dims,
+                                                     uint32_t range, double max_cells) {
     const uint32_t lane = lane_id();
-    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const uint32_t W = 2 * (uint32_t)dims + 1;
-    for (uint64_t sc = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; sc < nsc; sc += nw) {
-        const uint64_t a = offs[sc];
-        const uint64_t n = offs[sc + 1] > a ? offs[sc + 1] - a : 0;
+    {
         const uint64_t m = n < kTuneRows ? n : kTuneRows;
         uint32_t lo[2][3] = {{0, 0, 0}, {0, 0, 0}}, hi[2][3] = {{0, 0, 0}, {0, 0, 0}};
         bool ok[2] = {false, false};
@@ -144,7 +143,7 @@ __global__ void k_tune_scenes(const uint32_t* boxes, const unsigned long long* o
             for (int s = s0 - 2 > 0 ? s0 - 2 : 0; s <= 31; s++) {
                 if (s == s_win + 1 && best_cost < 1e300) break;
                 const double C = tune_cells(nrc_dev(range, s), dims);
-                if (C > 4.0e9) continue;
+                if (C > max_cells) continue;
                 if (s > s_win && C > fmax(4096.0, 64.0 * (double)n)) continue;
                 double e = 0, cm = 0;
 #pragma unroll
@@ -178,7 +177,17 @@ __global__ void k_tune_scenes(const uint32_t* boxes, const unsigned long long* o
                 best.est_entries = (double)n;
             }
         }
-        if (lane == 0) out[sc] = best;
+        return best;
+    }
+}
+
+__global__ void k_tune_scenes(const uint32_t* boxes, const unsigned long long* offs, uint32_t nsc, int dims,
+                              uint32_t range, SceneTune* out) {
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t sc = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; sc < nsc; sc += nw) {
+        const uint64_t a = offs[sc];
+        const SceneTune best = tune_scene_warp(boxes, a, offs[sc + 1] > a ? offs[sc + 1] - a : 0, dims, range, 4.0e9);
+        if (lane_id() == 0) out[sc] = best;
     }
 }
 
@@ -360,31 +369,29 @@ __global__ void k_zero_counts(Params pin) {
     for (uint64_t i = 4 * n4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.ncells; i += stride) p.counts[i] = 0;
 }
 
-template <int D, bool MERGED>
-__global__ void __launch_bounds__(kBoxThreads) k_count(Params pin) {
-    __shared__ __align__(16) uint32_t sbox[kBoxThreads * (2 * D + 1)];
-    const Params p = resolve(pin);
-    for (uint64_t b0 = (uint64_t)blockIdx.x * kBoxThreads; b0 < p.nboxes; b0 += (uint64_t)gridDim.x * kBoxThreads) {
+// tiles of kBoxThreads boxes: blk, blk + nblk, ... (blockDim.x == kBoxThreads)
+template <int D, bool SCATTER, bool MERGED>
+__device__ __forceinline__ void box_pass(const Params& p, uint32_t* sbox, uint64_t blk, uint64_t nblk) {
+    for (uint64_t b0 = blk * kBoxThreads; b0 < p.nboxes; b0 += nblk * kBoxThreads) {
         const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
-        if (p.box_copy) stage_upload<D>(p, b0, nb, sbox);
+        if (!SCATTER && p.box_copy) stage_upload<D>(p, b0, nb, sbox);
         else stage_boxes<D>(p, b0, nb, sbox);
         __syncthreads();
-        enumerate_cells<D, false, MERGED>(p, sbox, b0, nb);
+        enumerate_cells<D, SCATTER, MERGED>(p, sbox, b0, nb);
         __syncthreads();
     }
 }
 
 template <int D, bool MERGED>
+__global__ void __launch_bounds__(kBoxThreads) k_count(Params pin) {
+    __shared__ __align__(16) uint32_t sbox[kBoxThreads * (2 * D + 1)];
+    box_pass<D, false, MERGED>(resolve(pin), sbox, blockIdx.x, gridDim.x);
+}
+
+template <int D, bool MERGED>
 __global__ void __launch_bounds__(kBoxThreads) k_scatter(Params pin) {
     __shared__ __align__(16) uint32_t sbox[kBoxThreads * (2 * D + 1)];
-    const Params p = resolve(pin);
-    for (uint64_t b0 = (uint64_t)blockIdx.x * kBoxThreads; b0 < p.nboxes; b0 += (uint64_t)gridDim.x * kBoxThreads) {
-        const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
-        stage_boxes<D>(p, b0, nb, sbox);
-        __syncthreads();
-        enumerate_cells<D, true, MERGED>(p, sbox, b0, nb);
-        __syncthreads();
-    }
+    box_pass<D, true, MERGED>(resolve(pin), sbox, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -444,22 +451,28 @@ __device__ __forceinline__ unsigned long long warp_incl_scan64(unsigned long lon
     return v;
 }
 
+// cell r*128 + 4*lane of chunk `chunk`, chunks of Q rows of 128 cells
+template <int Q = 4>
 __device__ __forceinline__ uint64_t chunk_cell(uint64_t chunk, int r) {
-    return chunk * kScanChunk + (uint64_t)r * 128 + lane_id() * 4;
+    return chunk * (128u * Q) + (uint64_t)r * 128 + lane_id() * 4;
 }
 
-// the 16 counts of this lane's cells of the chunk (zeros past the end)
-__device__ __forceinline__ void scan_load(const Params& p, uint64_t chunk, uint32_t v[kScanPerThread]) {
-    const bool full = chunk * kScanChunk + kScanChunk <= p.ncells;
+// the 4*Q counts of this lane's cells of the chunk (zeros past the end);
+// PAST_L1: counts written by other blocks of the same launch
+template <int Q = 4, bool PAST_L1 = false>
+__device__ __forceinline__ void scan_load(const Params& p, uint64_t chunk, uint32_t (&v)[4 * Q]) {
+    const bool full = chunk * (128u * Q) + 128u * Q <= p.ncells;
 #pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const uint64_t c = chunk_cell(chunk, r);
+    for (int r = 0; r < Q; r++) {
+        const uint64_t c = chunk_cell<Q>(chunk, r);
         if (full) {
-            const uint4 q = *reinterpret_cast<const uint4*>(p.counts + c);
+            const uint4* a = reinterpret_cast<const uint4*>(p.counts + c);
+            const uint4 q = PAST_L1 ? __ldcg(a) : *a;
             v[4 * r] = q.x; v[4 * r + 1] = q.y; v[4 * r + 2] = q.z; v[4 * r + 3] = q.w;
         } else {
 #pragma unroll
-            for (int k = 0; k < 4; k++) v[4 * r + k] = c + k < p.ncells ? p.counts[c + k] : 0u;
+            for (int k = 0; k < 4; k++)
+                v[4 * r + k] = c + k < p.ncells ? (PAST_L1 ? __ldcg(p.counts + c + k) : p.counts[c + k]) : 0u;
         }
     }
 }
@@ -587,6 +600,112 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t pari
     return false;
 }
 
+// the cells of chunk ch (counts v; `base` entries before the chunk): each
+// cell's end (start + count) into its counter, each cell of two or more boxes
+// into its work list (one atomic per list and chunk), and the work
+// statistics into ws
+struct ScanStats {
+    unsigned long long tests = 0;
+    uint32_t half = 0, jobs = 0, max = 0;
+};
+
+// (pl: the kernel's own parameters, for the list tables: indexing a local
+// copy of Params with a run-time list number would move it to local memory)
+template <int Q = 4>
+__device__ __forceinline__ void scan_chunk(const Params& p, const Params& pl, uint64_t ch, bool full,
+                                           const uint32_t (&v)[4 * Q], unsigned long long base, ScanStats& ws) {
+    constexpr int kPer = 4 * Q;
+    const uint32_t lane = lane_id();
+    uint32_t big = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) big |= v[k] >> 1;
+    // row scans: the cells of row q before this lane's, and rows < q whole
+    uint32_t st[kPer];
+    unsigned long long wtot = 0;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const uint32_t rs = v[4 * q] + v[4 * q + 1] + v[4 * q + 2] + v[4 * q + 3];
+        const uint32_t inc = warp_incl_scan(rs);  // < 2^32 while the entry total is
+        unsigned long long run = base + wtot + (inc - rs);
+        wtot += __shfl_sync(FULL_MASK, inc, 31);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            st[4 * q + k] = (uint32_t)run;
+            run += v[4 * q + k];
+        }
+        // the cell's counter becomes its end (start + count), in place
+        const uint64_t c = chunk_cell<Q>(ch, q);
+        if (full) {
+            *reinterpret_cast<uint4*>(p.counts + c) = make_uint4(
+                st[4 * q] + v[4 * q], st[4 * q + 1] + v[4 * q + 1], st[4 * q + 2] + v[4 * q + 2], st[4 * q + 3] + v[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (c + k < p.ncells) p.counts[c + k] = st[4 * q + k] + v[4 * q + k];
+        }
+    }
+    if (__any_sync(FULL_MASK, big != 0)) {
+        // per-lane list counts: lists 0..5 in 10-bit fields of pk, list 6 in pk6
+        unsigned long long pk = 0;
+        uint32_t pk6 = 0;
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            if (v[k] >= 2u) {
+                const uint32_t c = class_of(v[k]);
+                if (c < 6u) pk += 1ull << (10u * c);
+                else pk6 += 1u;
+            }
+        }
+        const unsigned long long pinc = warp_incl_scan64(pk);
+        const uint32_t p6inc = warp_incl_scan(pk6);
+        unsigned long long pk_excl = pinc - pk;
+        uint32_t pk6_excl = p6inc - pk6;
+        // lane c < 7: this chunk's first place in list c
+        const unsigned long long ptot = __shfl_sync(FULL_MASK, pinc, 31);
+        const uint32_t p6tot = __shfl_sync(FULL_MASK, p6inc, 31);
+        uint32_t lbase = 0;
+        if (lane < kNumLists) {
+            const uint32_t x = lane < 6u ? (uint32_t)(ptot >> (10u * lane)) & 1023u : p6tot;
+            if (x) lbase = atomicAdd(&p.ctr->n_list[lane], x);
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const uint32_t c = v[k] >= 2u ? class_of(v[k]) : 0u;
+            const uint32_t b = __shfl_sync(FULL_MASK, lbase, c);
+            if (v[k] >= 2u) {
+                uint32_t rk;
+                if (c < 6u) {
+                    rk = (uint32_t)(pk_excl >> (10u * c)) & 1023u;
+                    pk_excl += 1ull << (10u * c);
+                } else {
+                    rk = pk6_excl++;
+                }
+                const uint64_t idx = (uint64_t)b + rk;
+                const uint32_t key = p.records ? (uint32_t)(chunk_cell<Q>(ch, k >> 2) + (k & 3)) : st[k];
+                if (idx < pl.list_cap[c]) p.lists[pl.list_off[c] + idx] = make_uint2(key, v[k]);
+                ws.tests += (unsigned long long)v[k] * (v[k] - 1u) / 2u;
+                ws.half += v[k] >> 1;  // n*n/2 = n(n-1)/2 + n/2, rounded down
+                ws.jobs += (v[k] + 255u) >> 8;
+                ws.max = max(ws.max, v[k]);
+            }
+        }
+    }
+}
+
+// the work statistics of a warp's cells (pair tests, and the reference's
+// numCompPairs, 256-row jobs and largest cell) into the counters
+__device__ __forceinline__ void scan_stats_flush(const Params& p, const ScanStats& st) {
+    const unsigned long long tests = warp_sum_u64(st.tests);
+    const unsigned long long half = warp_sum_u64(st.half), jobs = warp_sum_u64(st.jobs);
+    const uint32_t mx = __reduce_max_sync(FULL_MASK, st.max);
+    if (lane_id() == 0 && mx) {
+        atomicAdd(&p.ctr->tests, tests);
+        atomicAdd(&p.ctr->comp_pairs, tests + half);
+        atomicAdd(&p.ctr->jobs, jobs);
+        atomicMax(&p.ctr->max_cell, mx);
+    }
+}
+
 // k_scan_cells: each warp keeps its next chunk's counts in flight as a bulk
 // copy into one of two shared-memory buffers while it works on the current
 // one. A partial chunk (only the grid's last) is read with plain loads.
@@ -613,8 +732,7 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_scan_cells(Params pin) {
     };
     issue(0);
     issue(1);
-    unsigned long long st_tests = 0;
-    uint32_t st_half = 0, st_jobs = 0, st_max = 0;
+    ScanStats stats;
     for (uint64_t i = 0;; i++) {
         const uint64_t ch = first + i * nw;
         if (ch >= chunks) break;
@@ -647,93 +765,9 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_scan_cells(Params pin) {
         unsigned long long base = lane == 0 ? r.sum : 0ull;
         if (lane > 0 && lane <= ci) base = r.chunk[lane - 1];
         base = warp_sum_u64(base);
-        uint32_t big = 0;
-#pragma unroll
-        for (int k = 0; k < kScanPerThread; k++) big |= v[k] >> 1;
-        // row scans: the cells of row q before this lane's, and rows < q whole
-        uint32_t st[kScanPerThread];
-        const bool full = ch < full_chunks;
-        unsigned long long wtot = 0;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const uint32_t rs = v[4 * q] + v[4 * q + 1] + v[4 * q + 2] + v[4 * q + 3];
-            const uint32_t inc = warp_incl_scan(rs);  // < 2^32 while the entry total is
-            unsigned long long run = base + wtot + (inc - rs);
-            wtot += __shfl_sync(FULL_MASK, inc, 31);
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                st[4 * q + k] = (uint32_t)run;
-                run += v[4 * q + k];
-            }
-            // the cell's counter becomes its end (start + count), in place
-            const uint64_t c = chunk_cell(ch, q);
-            if (full) {
-                *reinterpret_cast<uint4*>(p.counts + c) = make_uint4(
-                    st[4 * q] + v[4 * q], st[4 * q + 1] + v[4 * q + 1], st[4 * q + 2] + v[4 * q + 2], st[4 * q + 3] + v[4 * q + 3]);
-            } else {
-#pragma unroll
-                for (int k = 0; k < 4; k++)
-                    if (c + k < p.ncells) p.counts[c + k] = st[4 * q + k] + v[4 * q + k];
-            }
-        }
-        if (__any_sync(FULL_MASK, big != 0)) {
-            // per-lane list counts: lists 0..5 in 10-bit fields of pk, list 6 in pk6
-            unsigned long long pk = 0;
-            uint32_t pk6 = 0;
-#pragma unroll
-            for (int k = 0; k < kScanPerThread; k++) {
-                if (v[k] >= 2u) {
-                    const uint32_t c = class_of(v[k]);
-                    if (c < 6u) pk += 1ull << (10u * c);
-                    else pk6 += 1u;
-                }
-            }
-            const unsigned long long pinc = warp_incl_scan64(pk);
-            const uint32_t p6inc = warp_incl_scan(pk6);
-            unsigned long long pk_excl = pinc - pk;
-            uint32_t pk6_excl = p6inc - pk6;
-            // lane c < 7: this chunk's first place in list c
-            const unsigned long long ptot = __shfl_sync(FULL_MASK, pinc, 31);
-            const uint32_t p6tot = __shfl_sync(FULL_MASK, p6inc, 31);
-            uint32_t lbase = 0;
-            if (lane < kNumLists) {
-                const uint32_t x = lane < 6u ? (uint32_t)(ptot >> (10u * lane)) & 1023u : p6tot;
-                if (x) lbase = atomicAdd(&p.ctr->n_list[lane], x);
-            }
-#pragma unroll
-            for (int k = 0; k < kScanPerThread; k++) {
-                const uint32_t c = v[k] >= 2u ? class_of(v[k]) : 0u;
-                const uint32_t b = __shfl_sync(FULL_MASK, lbase, c);
-                if (v[k] >= 2u) {
-                    uint32_t rk;
-                    if (c < 6u) {
-                        rk = (uint32_t)(pk_excl >> (10u * c)) & 1023u;
-                        pk_excl += 1ull << (10u * c);
-                    } else {
-                        rk = pk6_excl++;
-                    }
-                    const uint64_t idx = (uint64_t)b + rk;
-                    const uint32_t key = p.records ? (uint32_t)(chunk_cell(ch, k >> 2) + (k & 3)) : st[k];
-                    if (idx < pin.list_cap[c]) p.lists[pin.list_off[c] + idx] = make_uint2(key, v[k]);
-                    st_tests += (unsigned long long)v[k] * (v[k] - 1u) / 2u;
-                    st_half += v[k] >> 1;  // n*n/2 = n(n-1)/2 + n/2, rounded down
-                    st_jobs += (v[k] + 255u) >> 8;
-                    st_max = max(st_max, v[k]);
-                }
-            }
-        }
+        scan_chunk(p, pin, ch, ch < full_chunks, v, base, stats);
     }
-    // the work statistics of this warp's cells (pair tests, and the
-    // reference's numCompPairs, 256-row jobs and largest cell)
-    st_tests = warp_sum_u64(st_tests);
-    const unsigned long long half = warp_sum_u64(st_half), jobs = warp_sum_u64(st_jobs);
-    st_max = __reduce_max_sync(FULL_MASK, st_max);
-    if (lane == 0 && st_max) {
-        atomicAdd(&p.ctr->tests, st_tests);
-        atomicAdd(&p.ctr->comp_pairs, st_tests + half);
-        atomicAdd(&p.ctr->jobs, jobs);
-        atomicMax(&p.ctr->max_cell, st_max);
-    }
+    scan_stats_flush(p, stats);
 }
 
 // ---------------------------------------------------------------------------
@@ -742,9 +776,12 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_scan_cells(Params pin) {
 // ---------------------------------------------------------------------------
 constexpr uint32_t kTaskCols = 8;
 
-__global__ void k_expand(Params p) {
-    const uint32_t nh = mn64(p.ctr->n_list[kListHuge], p.list_cap[kListHuge]);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nh; i += gridDim.x * blockDim.x) {
+// huge cells i0, i0 + stride, ...
+// (the run counters that the passes read are read past L1: in a one-launch
+// query they change between phases of the same kernel)
+__device__ __forceinline__ void expand_cells(const Params& p, uint32_t i0, uint32_t stride) {
+    const uint32_t nh = mn64(__ldcg(&p.ctr->n_list[kListHuge]), p.list_cap[kListHuge]);
+    for (uint32_t i = i0; i < nh; i += stride) {
         const uint2 sn = p.lists[p.list_off[kListHuge] + i];
         const uint32_t n = sn.y;
         const uint32_t R = (n + 31) >> 5;
@@ -758,6 +795,8 @@ __global__ void k_expand(Params p) {
         if ((uint64_t)b + cnt > p.task_cap) atomicOr(&p.ctr->err, kErrTaskOvf);
     }
 }
+
+__global__ void k_expand(Params p) { expand_cells(p, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x); }
 
 // ---------------------------------------------------------------------------
 // pair test
@@ -1206,7 +1245,7 @@ __device__ __forceinline__ void small_items(const Params& p, const Slots& s, War
                                             uint64_t stride) {
     constexpr uint32_t G = 32 / WG;
     const uint32_t lane = lane_id(), g = lane / WG, r = lane % WG;
-    const uint64_t nl = mn64(p.ctr->n_list[list], p.list_cap[list]);
+    const uint64_t nl = mn64(__ldcg(&p.ctr->n_list[list]), p.list_cap[list]);
     const uint64_t nitems = (nl + G - 1) / G;
     for (uint64_t item = first; item < nitems; item += stride) {
         uint32_t n1, gid;
@@ -1221,14 +1260,13 @@ __device__ __forceinline__ void rec_hits(const Params& p, const WarpOut& o) {
     if (lane_id() == 0 && h) atomicAdd(&p.ctr->rec_pairs, h);
 }
 
-template <int D, bool BIP, bool NARROW, bool REC = false>
-__global__ void __launch_bounds__(kPairThreads, 5) k_pairs_small(Params p) {
-    __shared__ uint4 s_a[kPairWarps][kSmallSlots], s_b[kPairWarps][kSmallSlots];
-    __shared__ uint2 s_out[kPairWarps][kWarpOut];
-    const uint32_t warp = threadIdx.x >> 5;
-    const Slots s{s_a[warp], s_b[warp]};
-    WarpOut o{s_out[warp], 0, kWarpOut};
-    const uint64_t gw = (uint64_t)blockIdx.x * kPairWarps + warp, nw = (uint64_t)gridDim.x * kPairWarps;
+// the four small-cell lists, warp gw of nw; per-warp staging in s_a, s_b
+// (kSmallSlots each) and an output buffer of kWarpOut pairs
+template <int D, bool BIP, bool NARROW, bool REC>
+__device__ __forceinline__ void small_pass(const Params& p, uint4* s_a, uint4* s_b, uint2* s_out, uint64_t gw,
+                                           uint64_t nw) {
+    const Slots s{s_a, s_b};
+    WarpOut o{s_out, 0, kWarpOut};
     // classes interleaved over the warps so every warp gets a similar mix
     small_items<D, 32, BIP, NARROW, REC>(p, s, o, 3, gw, nw);
     small_items<D, 16, BIP, NARROW, REC>(p, s, o, 2, (gw + nw / 4) % nw, nw);
@@ -1236,6 +1274,15 @@ __global__ void __launch_bounds__(kPairThreads, 5) k_pairs_small(Params p) {
     small_items<D, 4, BIP, NARROW, REC>(p, s, o, 0, (gw + 3 * nw / 4) % nw, nw);
     wflush(p, o);
     if (REC) rec_hits(p, o);
+}
+
+template <int D, bool BIP, bool NARROW, bool REC = false>
+__global__ void __launch_bounds__(kPairThreads, 5) k_pairs_small(Params p) {
+    __shared__ uint4 s_a[kPairWarps][kSmallSlots], s_b[kPairWarps][kSmallSlots];
+    __shared__ uint2 s_out[kPairWarps][kWarpOut];
+    const uint32_t warp = threadIdx.x >> 5;
+    small_pass<D, BIP, NARROW, REC>(p, s_a[warp], s_b[warp], s_out[warp], (uint64_t)blockIdx.x * kPairWarps + warp,
+                                    (uint64_t)gridDim.x * kPairWarps);
 }
 
 // ---- medium cells: one per warp item, staged whole ---------------------------
@@ -1390,17 +1437,18 @@ __device__ __forceinline__ uint32_t diag_allow(uint32_t allow, uint32_t lane, ui
     return a;
 }
 
-template <int D, bool BIP, bool NARROW, bool REC = false>
-__global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    uint4* base = reinterpret_cast<uint4*>(smem_raw);
-    const Slots s{base + warp * 2 * kMedSlots, base + warp * 2 * kMedSlots + kMedSlots};
-    uint2* obuf = reinterpret_cast<uint2*>(base + kPairWarps * 2 * kMedSlots) + warp * kMedOut;
-    WarpOut o{obuf, 0, kMedOut};
-    const uint64_t nl = mn64(p.ctr->n_list[kListMed], p.list_cap[kListMed]);
-    const uint64_t nw = (uint64_t)gridDim.x * kPairWarps;
-    for (uint64_t item = (uint64_t)blockIdx.x * kPairWarps + warp; item < nl; item += nw) {
+// the medium-cell list, warp gw of nw; wsm: the warp's kMedWarpBytes of
+// shared memory (staging slots, then the output buffer)
+constexpr uint32_t kMedWarpBytes = kMedSlots * 2 * sizeof(uint4) + kMedOut * sizeof(uint2);
+
+template <int D, bool BIP, bool NARROW, bool REC>
+__device__ __forceinline__ void med_pass(const Params& p, unsigned char* wsm, uint64_t gw, uint64_t nw) {
+    const uint32_t lane = lane_id();
+    uint4* base = reinterpret_cast<uint4*>(wsm);
+    const Slots s{base, base + kMedSlots};
+    WarpOut o{reinterpret_cast<uint2*>(base + 2 * kMedSlots), 0, kMedOut};
+    const uint64_t nl = mn64(__ldcg(&p.ctr->n_list[kListMed]), p.list_cap[kListMed]);
+    for (uint64_t item = gw; item < nl; item += nw) {
         const uint2 sn = p.lists[p.list_off[kListMed] + item];
         const uint32_t gid = sn.x;  // record mode: the cell id (its start is in the counters)
         const uint32_t start = REC ? (gid < p.ncells ? p.counts[gid] : 0xffffffffu) : sn.x;
@@ -1478,6 +1526,14 @@ __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
     }
     wflush(p, o);
     if (REC) rec_hits(p, o);
+}
+
+template <int D, bool BIP, bool NARROW, bool REC = false>
+__global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const uint32_t warp = threadIdx.x >> 5;
+    med_pass<D, BIP, NARROW, REC>(p, smem_raw + warp * kMedWarpBytes, (uint64_t)blockIdx.x * kPairWarps + warp,
+                                  (uint64_t)gridDim.x * kPairWarps);
 }
 
 // ---- big cells (block staged) and huge cells (tiles) -----------------------
@@ -1588,7 +1644,7 @@ __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const Slots sl{s.a, s.b};
     auto emit = [&](uint32_t ma, auto pa, uint32_t mb, auto pb, uint32_t myid) { bemit<BIP>(p, s, ma, pa, mb, pb, myid); };
-    const uint64_t nl = mn64(p.ctr->n_list[kListBig], p.list_cap[kListBig]);
+    const uint64_t nl = mn64(__ldcg(&p.ctr->n_list[kListBig]), p.list_cap[kListBig]);
     uint64_t cur = task * kBigCellsPerTask;
     const uint64_t end = mn64(cur + kBigCellsPerTask, nl);
     while (cur < end) {
@@ -1669,7 +1725,7 @@ template <int D, bool BIP, bool NARROW, bool REC>
 __device__ __forceinline__ void huge_item(const Params& p, BlockSmem& s, uint64_t item, uint32_t slot0) {
     const uint32_t lane = lane_id();
     const Slots sl{s.a, s.b};
-    const uint64_t nt = mn64(p.ctr->need_tasks, p.task_cap);
+    const uint64_t nt = mn64(__ldcg(&p.ctr->need_tasks), p.task_cap);
     if (item >= nt) return;
     const uint4 tk = p.tasks[item];
     const uint32_t gid = tk.x;  // record mode: the cell id; its start is in the counters
@@ -1722,29 +1778,28 @@ __device__ __forceinline__ void huge_item(const Params& p, BlockSmem& s, uint64_
     }
 }
 
-template <int D, bool BIP, bool NARROW, bool REC = false>
-__global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    BlockSmem& s = *reinterpret_cast<BlockSmem*>(smem_raw);
+// big-cell tasks and huge-cell tile tasks, block blk of nblk
+template <int D, bool BIP, bool NARROW, bool REC>
+__device__ __forceinline__ void block_pass(const Params& p, BlockSmem& s, uint64_t blk, uint64_t nblk) {
     const uint32_t t = threadIdx.x, warp = t >> 5;
     if (t == 0) {
         s.out_n = 0;
         s.first_ovf = kBlockOut;
         s.hits = 0;
-        const uint64_t nb = mn64(p.ctr->n_list[kListBig], p.list_cap[kListBig]);
-        const uint64_t nt = mn64(p.ctr->need_tasks, p.task_cap);
+        const uint64_t nb = mn64(__ldcg(&p.ctr->n_list[kListBig]), p.list_cap[kListBig]);
+        const uint64_t nt = mn64(__ldcg(&p.ctr->need_tasks), p.task_cap);
         s.nbt[0] = (nb + kBigCellsPerTask - 1) / kBigCellsPerTask;
         s.nbt[1] = (nt + kPairWarps - 1) / kPairWarps;
     }
     __syncthreads();
     const uint64_t total = s.nbt[0] + s.nbt[1];
-    for (uint64_t bt = blockIdx.x; bt < total; bt += gridDim.x) {
+    for (uint64_t bt = blk; bt < total; bt += nblk) {
         if (bt < s.nbt[0]) big_task<D, BIP, NARROW, REC>(p, s, bt);
         else huge_item<D, BIP, NARROW, REC>(p, s, (bt - s.nbt[0]) * kPairWarps + warp, warp * 64);
         __syncthreads();
         const uint32_t on = s.out_n, ovf = s.first_ovf;
         const uint32_t nv = min(on, ovf);
-        const bool last = bt + gridDim.x >= total;
+        const bool last = bt + nblk >= total;
         if (nv >= kBlockOut / 2 || on > nv || (last && on > 0)) {
             if (t == 0) s.gbase = nv ? atomicAdd(&p.ctr->pairs, (unsigned long long)nv) : 0ull;
             __syncthreads();
@@ -1758,6 +1813,12 @@ __global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
         }
     }
     if (REC && t == 0 && s.hits) atomicAdd(&p.ctr->rec_pairs, s.hits);
+}
+
+template <int D, bool BIP, bool NARROW, bool REC = false>
+__global__ void __launch_bounds__(kPairThreads, 2) k_pairs_block(Params p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    block_pass<D, BIP, NARROW, REC>(p, *reinterpret_cast<BlockSmem*>(smem_raw), blockIdx.x, gridDim.x);
 }
 
 // record mode, after the pair kernels: entries become the plain box indices
@@ -1858,13 +1919,340 @@ __global__ void __launch_bounds__(1024) k_scene_offsets(Params pin, const unsign
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// one-launch queries of small scenes: a cooperative launch whose blocks run
+// the whole pipeline, phase after phase, separated by grid barriers
+//   P0   every block: the cell size (warp 0 runs the tuner's model on 64
+//        sampled boxes: the same choice in every block) and the scene in
+//        shared memory; block 0 the chosen grid for the host and the next
+//        launch's zeroed run counters; the counters are zeroed first only
+//        when they may hold anything else (one more barrier)
+//   P1   count
+//   P2   entry totals of chunks -- a small grid's (128-cell chunks)
+//        computed by every block itself, a larger one's (512-cell chunks) by
+//        all blocks (one more barrier) -- then the chunk prefixes in shared
+//        memory, and each warp's chunks' cell ends, work lists, statistics;
+//        a small grid's cell ends go to a buffer of their own, since other
+//        blocks may still be reading the counters
+//   P3   expand and scatter
+//   P4   small, medium and block pair passes; the grid's counters zeroed for
+//        the next launch; the last block to finish copies the run counters
+//        to the host
+// Data written in one phase and read in a later one is read past L1. A
+// barrier's wait is bounded: a block that gives up sets kErrWait and leaves,
+// and the others give up at their next barrier.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kFusedThreads = kPairThreads;
+constexpr uint32_t kFusedChunks = (uint32_t)(kFusedMaxCells / kScanChunk);
+constexpr uint32_t kFusedLocalCells = 8192;  // grids of up to 8192 cells: 128-cell chunks, totals per block
+constexpr uint32_t kGridWaitLimit = 1u << 20;  // polls of 64 ns or more: the wait ends after a second at most
+constexpr uint32_t kSmallWarpBytes = 2 * kSmallSlots * sizeof(uint4) + kWarpOut * sizeof(uint2);
+static_assert(kFusedThreads == kBoxThreads, "box tiles of one block");
+static_assert(kFusedChunks % kFusedThreads == 0, "chunk prefixes per thread");
+
+// barrier number k of this launch (k counts the barriers passed so far)
+__device__ __forceinline__ bool grid_barrier(const FusedArgs& a, uint32_t k) {
+    __shared__ uint32_t s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("red.release.gpu.add.u32 [%0], 1;" ::"l"(a.bar) : "memory");
+        const uint32_t target = (k + 1) * gridDim.x;
+        uint32_t ok = 0;
+        for (uint32_t i = 0; i < kGridWaitLimit; i++) {
+            uint32_t v;
+            asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(a.bar) : "memory");
+            if ((int32_t)(v - a.bar_base) >= (int32_t)target) {
+                ok = 1;
+                break;
+            }
+            if (i >= 64) __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0u;
+}
+
+// the tuner's model (k_tune_scenes) for one scene of n boxes at row 0, in
+// single precision over exact integer sums: the one-launch path cannot wait
+// for double-precision divisions. Grids of at most max_cells cells, so a
+// box covers at most max_cells cells and every per-box product fits 32 bits.
+__device__ __forceinline__ uint32_t tune_scene_fast(const uint32_t* boxes, uint64_t n, int dims, uint32_t range,
+                                                    uint64_t max_cells) {
+    const uint32_t lane = lane_id();
+    const uint32_t W = 2 * (uint32_t)dims + 1;
+    const uint64_t m = n < kTuneRows ? n : kTuneRows;
+    uint32_t lo[2][3] = {{0, 0, 0}, {0, 0, 0}}, hi[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    bool ok[2] = {false, false};
+    unsigned long long ext = 0, good = 0;
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const uint64_t k = lane + 32u * j;
+        if (k >= m) continue;
+        const uint32_t* b = boxes + (k * n / m) * W;
+        bool v = true;
+        for (int d = 0; d < dims; d++) {
+            lo[j][d] = __ldg(b + 2 * d);
+            hi[j][d] = __ldg(b + 2 * d + 1);
+            v = v && lo[j][d] <= hi[j][d] && hi[j][d] < range;
+        }
+        ok[j] = v;
+        if (v) {
+            for (int d = 0; d < dims; d++) ext += (unsigned long long)(hi[j][d] - lo[j][d]) + 1;
+            good++;
+        }
+    }
+    ext = warp_sum_u64(ext);
+    good = warp_sum_u64(good);
+    // s0 = floor(log2(mean extent)), 0 below 2
+    const unsigned long long mean = ext / ((good ? good : 1ull) * (unsigned long long)dims);
+    const int s0 = mean < 2 ? 0 : 63 - __clzll(mean);
+    const int s_win = s0 + 3 < 31 ? s0 + 3 : 31;
+    const float scale = (float)n / (float)(m ? m : 1);
+    const uint64_t far_cap = n * 64 > 4096 ? n * 64 : 4096;
+    float best_cost = 3.0e38f;
+    uint32_t best = 0xffffffffu;
+    for (int s = s0 - 2 > 0 ? s0 - 2 : 0; s <= 31 && m > 0; s++) {
+        if (s == s_win + 1 && best != 0xffffffffu) break;
+        const uint64_t nrc = nrc_dev(range, s);
+        if (nrc > max_cells) continue;
+        const uint64_t C = dims == 3 ? nrc * nrc * nrc : nrc * nrc;  // nrc <= 2^20: no overflow in 64 bits
+        if (C > max_cells) continue;
+        if (s > s_win && C > far_cap) continue;
+        uint32_t e = 0;
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            if (!ok[j]) continue;
+            uint32_t c = 1;
+            for (int d = 0; d < dims; d++) c *= (hi[j][d] >> s) - (lo[j][d] >> s) + 1;
+            e += c;  // <= 2 * max_cells
+        }
+        e = __reduce_add_sync(FULL_MASK, e);
+        if (e > 64u * (uint32_t)m) continue;
+        const float E = (float)e * scale, Cf = (float)C;
+        const float T = E * E / (2.0f * Cf);
+        const float occ = 2.0f * T / (E > 1.0f ? E : 1.0f) + 1.0f;
+        const float f = occ / (float)kTuneOcc > 1.0f ? occ / (float)kTuneOcc : 1.0f;
+        const float cost = (float)kTuneCell * Cf + (float)kTuneEntry * E + (float)kTuneTest * f * T;
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = (uint32_t)s;
+        }
+    }
+    if (best == 0xffffffffu) {  // the coarsest grid that is not a single cell
+        uint32_t s = 31;
+        while (s > 0 && nrc_dev(range, (int)s - 1) <= 1) s--;
+        best = s;
+    }
+    return best;
+}
+
+template <int D, bool NARROW>
+__global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArgs a) {
+    Params p = pin;  // the grid's size is set below
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_shift;
+    __shared__ Scene s_scene;
+    __shared__ unsigned long long s_wsum[kPairWarps];
+    __shared__ uint32_t s_csum[kFusedLocalCells / 128];
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    const uint64_t blk = blockIdx.x, nblk = gridDim.x;
+    const uint64_t gw = blk * kPairWarps + warp, nw = nblk * kPairWarps;
+    const uint64_t gt = blk * kFusedThreads + t, nt = nblk * kFusedThreads;
+    const uint32_t range = p.max_range;
+    uint32_t nbar = 0;
+    if (blk == 0 && t == 0) {
+        unsigned long long now;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+        p.ctr->t_start = now;
+    }
+#define FUSED_BARRIER()                                        \
+    if (!grid_barrier(a, nbar++)) {                            \
+        if (t == 0) atomicOr(&p.ctr->err, (unsigned)kErrWait); \
+        return;                                                \
+    }
+    // P0
+    if (warp == 0) {
+        uint32_t sh = a.shift;
+        if (sh == kFusedTune) sh = tune_scene_fast(p.boxes, p.nboxes, D, range, kFusedMaxCells);
+        if (lane == 0) s_shift = sh;
+    }
+    __syncthreads();
+    const uint32_t shift = s_shift, nrc = nrc_dev(range, (int)shift);
+    p.ncells = D == 3 ? (uint64_t)nrc * nrc * nrc : (uint64_t)nrc * nrc;
+    if (t == 0) s_scene = Scene{0u, (uint32_t)p.nboxes, shift, nrc, 0ull, range, 0u};
+    if (blk == 0 && t == 0) {
+        *a.ctr_next = Ctr{};
+        p.ctr->cells = p.ncells;
+        p.ctr->shift = shift;
+        a.scenes[0] = Scene{0u, (uint32_t)p.nboxes, shift, nrc, 0ull, range, 0u};
+    }
+    __syncthreads();
+    p.scenes = &s_scene;  // the count and the scatter read the scene from shared memory
+    if (a.zero_cells) {
+        uint4* c4 = reinterpret_cast<uint4*>(p.counts);
+        for (uint64_t i = gt; i < a.zero_cells / 4; i += nt) c4[i] = make_uint4(0u, 0u, 0u, 0u);
+        for (uint64_t i = 4 * (a.zero_cells / 4) + gt; i < a.zero_cells; i += nt) p.counts[i] = 0u;
+        FUSED_BARRIER()
+    }
+    // P1: count
+    uint32_t* sbox = reinterpret_cast<uint32_t*>(smem_raw);
+    box_pass<D, false, false>(p, sbox, blk, nblk);
+    FUSED_BARRIER()
+    // P2: chunk entry totals and prefixes, then the cells
+    uint32_t* pre = reinterpret_cast<uint32_t*>(smem_raw);
+    unsigned long long total = 0;
+    bool fits;
+    if (p.ncells <= kFusedLocalCells) {
+        const uint32_t nch = (uint32_t)((p.ncells + 127) / 128);
+        for (uint32_t ch = warp; ch < nch; ch += kPairWarps) {
+            uint32_t v[4];
+            scan_load<1, true>(p, ch, v);
+            s_csum[ch] = __reduce_add_sync(FULL_MASK, v[0] + v[1] + v[2] + v[3]);  // < 2^32 (at most 2^25)
+        }
+        __syncthreads();
+        if (t == 0) {
+            unsigned long long run = 0;
+            for (uint32_t ch = 0; ch < nch; ch++) {
+                pre[ch] = (uint32_t)run;  // < entry_cap when it is used
+                run += s_csum[ch];
+            }
+            s_wsum[0] = run;
+        }
+        __syncthreads();
+        total = s_wsum[0];
+        fits = total <= p.entry_cap;
+        if (fits) {
+            // the cell ends go to a buffer of their own: other blocks may
+            // still be summing the counters
+            Params pe = p;
+            pe.counts = a.ends;
+            ScanStats ws;
+            const uint64_t full = p.ncells / 128;
+            for (uint64_t ch = gw; ch < nch; ch += nw) {
+                uint32_t v[4];
+                scan_load<1, true>(p, ch, v);
+                scan_chunk<1>(pe, pin, ch, ch < full, v, pre[ch], ws);
+            }
+            scan_stats_flush(p, ws);
+        }
+    } else {
+        const uint64_t nch = (p.ncells + kScanChunk - 1) / kScanChunk;
+        for (uint64_t ch = gw; ch < nch; ch += nw) {
+            uint32_t v[kScanPerThread];
+            scan_load<4, true>(p, ch, v);
+            uint32_t sum = 0;  // < 2^32: a chunk holds at most 512 cells of at most kFusedMaxBoxes entries
+#pragma unroll
+            for (int k = 0; k < kScanPerThread; k++) sum += v[k];
+            sum = __reduce_add_sync(FULL_MASK, sum);
+            if (lane == 0) a.chunk_sum[ch] = sum;
+        }
+        FUSED_BARRIER()
+        constexpr uint32_t kPer = kFusedChunks / kFusedThreads;
+        uint32_t x[kPer];
+        unsigned long long sum = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; k++) {
+            const uint64_t i = (uint64_t)t * kPer + k;
+            x[k] = i < nch ? __ldcg(a.chunk_sum + i) : 0u;
+            sum += x[k];
+        }
+        const unsigned long long incl = warp_incl_scan64(sum);
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        unsigned long long run = incl - sum;
+#pragma unroll
+        for (uint32_t w = 0; w < kPairWarps; w++) {
+            if (w < warp) run += s_wsum[w];
+            total += s_wsum[w];
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; k++) {
+            const uint64_t i = (uint64_t)t * kPer + k;
+            if (i < nch) pre[i] = (uint32_t)run;  // < entry_cap when it is used
+            run += x[k];
+        }
+        __syncthreads();
+        fits = total <= p.entry_cap;
+        if (fits) {
+            ScanStats ws;
+            const uint64_t full = p.ncells / kScanChunk;
+            for (uint64_t ch = gw; ch < nch; ch += nw) {
+                uint32_t v[kScanPerThread];
+                scan_load<4, true>(p, ch, v);
+                scan_chunk(p, pin, ch, ch < full, v, pre[ch], ws);
+            }
+            scan_stats_flush(p, ws);
+        }
+    }
+    if (blk == 0 && t == 0) {
+        p.ctr->entries = total;
+        if (!fits) atomicOr(&p.ctr->err, (unsigned)kErrEntryOvf);
+    }
+    FUSED_BARRIER()
+    // P3: tile tasks of huge cells, scatter (against the cell ends)
+    if (fits) {
+        expand_cells(p, (uint32_t)gt, (uint32_t)nt);
+        Params pe = p;
+        if (p.ncells <= kFusedLocalCells) pe.counts = a.ends;
+        box_pass<D, true, false>(pe, sbox, blk, nblk);
+    }
+    FUSED_BARRIER()
+#undef FUSED_BARRIER
+    // P4: the counters zeroed for the next launch (the pair passes read the
+    // work lists, not the counters), then the pairs
+    {
+        uint4* c4 = reinterpret_cast<uint4*>(p.counts);
+        for (uint64_t i = gt; i < p.ncells / 4; i += nt) c4[i] = make_uint4(0u, 0u, 0u, 0u);
+        for (uint64_t i = 4 * (p.ncells / 4) + gt; i < p.ncells; i += nt) p.counts[i] = 0u;
+    }
+    if (fits) {
+        unsigned char* ws = smem_raw + warp * kSmallWarpBytes;
+        uint4* sa = reinterpret_cast<uint4*>(ws);
+        small_pass<D, false, NARROW, false>(p, sa, sa + kSmallSlots, reinterpret_cast<uint2*>(sa + 2 * kSmallSlots),
+                                            gw, nw);
+        __syncthreads();
+        med_pass<D, false, NARROW, false>(p, smem_raw + warp * kMedWarpBytes, gw, nw);
+        __syncthreads();
+        block_pass<D, false, NARROW, false>(p, *reinterpret_cast<BlockSmem*>(smem_raw), blk, nblk);
+    }
+    // the last block to finish copies the run counters to the host (one
+    // more arrival per block on the barriers' count)
+    __syncthreads();
+    if (t == 0) {
+        __threadfence();
+        uint32_t old;
+        asm volatile("atom.acq_rel.gpu.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(a.bar) : "memory");
+        if ((int32_t)(old - a.bar_base) == (int32_t)((nbar + 1) * nblk - 1)) {
+            __threadfence();
+            constexpr uint32_t kWords = sizeof(Ctr) / sizeof(unsigned long long);
+            static_assert(sizeof(Ctr) % sizeof(unsigned long long) == 0, "run counters in 8-byte words");
+            const unsigned long long* src = reinterpret_cast<const unsigned long long*>(p.ctr);
+            unsigned long long w[kWords];
+#pragma unroll
+            for (uint32_t k = 0; k < kWords; k++) w[k] = __ldcg(src + k);
+            Ctr* h = a.ctr_host;
+            unsigned long long* dst = reinterpret_cast<unsigned long long*>(h);
+#pragma unroll
+            for (uint32_t k = 0; k < kWords; k++) dst[k] = w[k];
+            h->barriers = nbar + 1;
+            unsigned long long now;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+            h->t_end = now;
+            __threadfence_system();
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 static int g_blocks_small = 1, g_blocks_med = 1, g_blocks_block = 1;
 static int g_sm_count = 0;
 
-static size_t med_smem() { return (size_t)kPairWarps * (2 * kMedSlots * sizeof(uint4) + kMedOut * sizeof(uint2)); }
+static size_t med_smem() { return (size_t)kPairWarps * kMedWarpBytes; }
 
 size_t pair_smem_bytes() { return sizeof(BlockSmem); }
 
@@ -1874,6 +2262,40 @@ static cudaError_t init_variant() {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_pairs_block<D, B, N, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BlockSmem));
     return e;
+}
+
+static int g_fused_blocks = 0;
+
+static size_t fused_smem() {
+    size_t b = (size_t)kPairWarps * kMedWarpBytes;
+    b = b > sizeof(BlockSmem) ? b : sizeof(BlockSmem);
+    b = b > (size_t)kPairWarps * kSmallWarpBytes ? b : (size_t)kPairWarps * kSmallWarpBytes;
+    b = b > (size_t)kFusedChunks * 4 ? b : (size_t)kFusedChunks * 4;
+    b = b > (size_t)kBoxThreads * 7 * 4 ? b : (size_t)kBoxThreads * 7 * 4;
+    return b;
+}
+
+int fused_blocks() { return g_fused_blocks; }
+
+template <int D, bool N>
+static cudaError_t launch_fused_t(const Params& p, const FusedArgs& a, cudaStream_t st) {
+    Params pp = p;
+    FusedArgs aa = a;
+    void* args[] = {&pp, &aa};
+    return cudaLaunchCooperativeKernel((const void*)k_fused<D, N>, dim3((unsigned)g_fused_blocks), dim3(kFusedThreads),
+                                      args, fused_smem(), st);
+}
+
+cudaError_t launch_fused(const Params& p, const FusedArgs& a, int dims, cudaStream_t st) {
+    if (g_fused_blocks <= 0) return cudaErrorNotSupported;
+    const bool narrow = p.max_range <= (1u << kMissShift);
+    if (narrow) return dims == 2 ? launch_fused_t<2, true>(p, a, st) : launch_fused_t<3, true>(p, a, st);
+    return dims == 2 ? launch_fused_t<2, false>(p, a, st) : launch_fused_t<3, false>(p, a, st);
+}
+
+template <int D, bool N>
+static cudaError_t init_fused() {
+    return cudaFuncSetAttribute(k_fused<D, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem());
 }
 
 cudaError_t kernels_init() {
@@ -1902,6 +2324,20 @@ cudaError_t kernels_init() {
     g_blocks_med = nb > 0 ? nb : 1;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs_block<3, false, true>, kPairThreads, sizeof(BlockSmem))) != cudaSuccess) return e;
     g_blocks_block = nb > 0 ? nb : 1;
+    // one-launch queries: one block per SM, all resident (cooperative launch)
+    if ((e = init_fused<2, true>()) != cudaSuccess) return e;
+    if ((e = init_fused<3, true>()) != cudaSuccess) return e;
+    if ((e = init_fused<2, false>()) != cudaSuccess) return e;
+    if ((e = init_fused<3, false>()) != cudaSuccess) return e;
+    {
+        int dev = 0, coop = 0, nf = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nf, k_fused<3, true>, kFusedThreads, fused_smem())) !=
+            cudaSuccess)
+            return e;
+        g_fused_blocks = coop && nf >= 1 ? g_sm_count : 0;
+    }
     return cudaSuccess;
 }
 

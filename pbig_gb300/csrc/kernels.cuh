@@ -122,6 +122,10 @@ struct Ctr {
     unsigned long long comp_pairs;      // sum of n*n/2 over cells of n >= 2 (the reference's numCompPairs)
     unsigned long long jobs;            // sum of ceil(n/256) over cells of n >= 2 (its 256-row jobs)
     unsigned long long rec_pairs;       // record mode: pairs in the records (pairs counts 8-byte words)
+    unsigned long long cells;           // one-launch queries: cells of the grid the kernel chose
+    unsigned int shift;                 // one-launch queries: its cell shift
+    unsigned int barriers;              // one-launch queries: grid barriers the launch passed
+    unsigned long long t_start, t_end;  // one-launch queries: device time (ns) at the start and the end
 };
 
 // query sizes read from device memory (graph replays: one captured graph
@@ -212,5 +216,37 @@ uint64_t scan_tiles(uint64_t ncells);
 size_t scan_state_bytes(uint64_t ncells);  // scan tile records
 size_t pair_smem_bytes();
 cudaError_t kernels_init();
+
+// ---- one-launch queries of small scenes -----------------------------------
+// A self query of at most kFusedMaxBoxes boxes runs as one cooperative
+// launch: the cell size (chosen on the device when `shift` is kFusedTune,
+// grids of at most kFusedMaxCells cells), the count, the scan, the scatter
+// and every pair pass, separated by grid barriers whose waits are bounded
+// (kErrWait). p must carry the device boxes, counts (kFusedMaxCells or the
+// given grid), entries, lists, tasks, out and ctr, whose counters must be
+// zero at launch; the kernel zeroes ctr_next for the launch after it, writes
+// the chosen grid (ctr->cells, ctr->shift) and the scene table for the host,
+// leaves the counters of its grid zero, and its last block to finish copies
+// the run counters to ctr_host with the number of barrier arrivals per block
+// the launch made (ctr_host->barriers; unchanged when a wait gave up). Counters that may hold anything else (another pipeline
+// used them, or they are new) are zeroed first when zero_cells says so.
+constexpr uint64_t kFusedMaxBoxes = 1u << 18;
+constexpr uint64_t kFusedMaxCells = 1u << 20;
+constexpr uint32_t kFusedTune = 0xffffffffu;
+
+struct FusedArgs {
+    unsigned int* bar;        // arrival counter of the grid barriers (only ever increases)
+    unsigned int bar_base;    // its value when the launch starts
+    uint32_t* chunk_sum;      // entry totals of 512-cell chunks (kFusedMaxCells / 512 words)
+    uint32_t* ends;           // cell ends of grids of at most 8192 cells (8192 words)
+    Scene* scenes;            // the scene table for the host, written by the kernel
+    Ctr* ctr_next;            // the run counters of the next launch (zeroed by this one)
+    Ctr* ctr_host;            // page-locked host copy of the final counters, written by the last block
+    uint64_t zero_cells;      // counters to zero before the count (0: they are zero)
+    uint32_t shift;           // the cell shift, or kFusedTune
+};
+// blocks of a one-launch query (0: not available on this device)
+int fused_blocks();
+cudaError_t launch_fused(const Params& p, const FusedArgs& a, int dims, cudaStream_t st);
 
 }  // namespace pbig

@@ -338,6 +338,11 @@ class Engine:
         quarter; negative: one after another)."""
         _check(self._L.pbig2_set_option(self._ctx, 4, int(sms)))
 
+    def set_one_launch(self, on: bool) -> None:
+        """Run small self queries (at most 262 144 boxes) as one cooperative
+        kernel launch (on by default); off: the regular pipeline."""
+        _check(self._L.pbig2_set_option(self._ctx, 5, int(bool(on))))
+
     def set_graphs(self, on: bool) -> None:
         """Capture/replay batched queries as CUDA graphs (on by default)."""
         _check(self._L.pbig2_set_option(self._ctx, 1, int(bool(on))))

@@ -51,6 +51,21 @@ def _fits(shift):
     return ((RANGE >> shift) ** 3) < (1 << 26)
 
 
+@pytest.fixture(autouse=True)
+def _regular_pipeline(request):
+    """The rerun belongs to the regular pipeline: a one-launch query's grid
+    has at most 2^20 cells, so no box can cover 2^26 of them."""
+    if "engine" not in request.fixturenames:
+        yield
+        return
+    eng = request.getfixturevalue("engine")
+    eng.set_one_launch(False)
+    try:
+        yield
+    finally:
+        eng.set_one_launch(True)
+
+
 def test_tuner_picks_a_size_the_spanning_box_overflows():
     """(CPU) The scene really exercises the rerun: the tuner's sample misses
     the spanning box and its choice is too fine for it."""
@@ -77,6 +92,7 @@ def test_self_query_reruns_on_a_coarser_grid(loc):
     else:
         src = torch.from_numpy(b.view(np.int32)).cuda()
     with Engine(0) as engine:
+        engine.set_one_launch(False)
         n = engine.self_intersect(src, RANGE)
         st = engine.stats()
         assert n == len(want)
@@ -163,12 +179,14 @@ def test_batch_with_one_spanning_box_reruns_every_scene(engine, loc):
 @pytest.mark.gpu
 def test_legacy_api_with_cs_zero_reruns(tmp_path):
     """pbig_init(num, range, cs = 0, ...) + pbig_check through a recording
-    report: three steps, each the brute-force pair set."""
+    report: three steps, each the oracle's pair set. The scene has 300 001
+    boxes, more than a one-launch query takes, so the regular pipeline and
+    its rerun serve it."""
     d = os.path.join(HERE, "clients", "recording")
     exe = build.compile_client([os.path.join(HERE, "clients", "legacy_client.cc"), os.path.join(d, "report.cc")],
                                str(tmp_path / "client"), include_first=[d])
-    b = _scene()
-    want = O.brute_pairs(b)
+    b = _scene(n=300001)
+    want, _ = O.grid_pairs(b, RANGE, cs=1 << 12)
     f = tmp_path / "boxes.bin"
     b.tofile(f)
     env = dict(os.environ, PBIG_PAIRS_OUT=str(tmp_path / "pairs.bin"))

@@ -186,13 +186,25 @@ def test_direct_pair_output(engine):
     assert engine.self_intersect(boxes, gen.RANGE) == n and not engine.result_in(out)
 
 
+@pytest.fixture
+def regular(engine):
+    """The shared context with every query on the regular multi-launch
+    pipeline (small self queries otherwise run as one launch)."""
+    engine.set_one_launch(False)
+    try:
+        yield engine
+    finally:
+        engine.set_one_launch(True)
+
+
 @pytest.mark.parametrize("split", [-1, 0, 8, 100])
-def test_host_output_split(engine, split):
+def test_host_output_split(regular, split):
     """Pairs to page-locked host memory with the small-cell and block kernels
     beside the medium-cell kernel (any SM share) or after it: the same pair
     set, self and red/blue, with cells of every class (a stack of identical
     boxes fills the block kernel)."""
     import torch
+    engine = regular
     boxes = gen.clustered3d(200000, seed=9)
     stack = np.repeat(boxes[:1], 3000, axis=0)
     boxes = np.concatenate([boxes, stack])
@@ -217,13 +229,17 @@ def test_host_output_split(engine, split):
         engine.set_host_split(0)
 
 
+@pytest.mark.parametrize("one_launch", [False, True])
 @pytest.mark.parametrize("dims", [2, 3])
-def test_pinned_host_input(engine, dims):
+def test_pinned_host_input(engine, dims, one_launch):
     """Page-locked host input is uploaded by the count kernel itself (no copy
-    before the pipeline): the same pairs as pageable input for self and
-    red/blue queries of ragged sizes (a count tile straddles red and blue),
-    with one side pinned and the other pageable, and in merged mode."""
+    before the pipeline; a one-launch query copies it first): the same pairs
+    as pageable input for self and red/blue queries of ragged sizes (a count
+    tile straddles red and blue), with one side pinned and the other
+    pageable, and in merged mode."""
     import torch
+    engine.set_one_launch(one_launch)
+    request_cleanup = engine.set_one_launch
 
     def pin(a):
         return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).pin_memory()
@@ -247,6 +263,7 @@ def test_pinned_host_input(engine, dims):
         assert np.array_equal(canon(engine.pairs()), want)
     finally:
         engine.set_merged(False)
+        request_cleanup(True)
 
 
 def test_output_capacity_growth(engine):
