@@ -304,8 +304,11 @@ def run_gb300(args, rank, local, ws):
     parts = boxes if isinstance(boxes, tuple) else (boxes,)
     dev = [torch.from_numpy(b.view(np.int32)).to(f"cuda:{local}") for b in parts]
     host = [torch.from_numpy(b.view(np.int32)).pin_memory() for b in parts]
-    stream = torch.cuda.current_stream()
+    # one stream for the L2 flush, the timing events and the queries, so
+    # that each timed query starts after the flush and the events bracket it
+    stream = torch.cuda.Stream(device=f"cuda:{local}")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")  # > L2 (129 MB)
+    torch.cuda.synchronize()
     eng = Engine(local)
 
     def query(src):
@@ -326,7 +329,8 @@ def run_gb300(args, rank, local, ws):
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
-            flush.zero_()
+            with torch.cuda.stream(stream):
+                flush.zero_()
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(stream)

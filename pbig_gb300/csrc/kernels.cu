@@ -776,11 +776,17 @@ __global__ void __launch_bounds__(kScanThreads, 4) k_scan_cells(Params pin) {
 // ---------------------------------------------------------------------------
 constexpr uint32_t kTaskCols = 8;
 
+// a run counter that a pass reads: FRESH (one-launch queries, where phases
+// of the same kernel change the counters) reads it past L1; the separate
+// kernels of the regular pipeline read it plainly (a load past L1 there
+// measured 20 % slower medium-cell and twice slower block passes)
+template <bool FRESH>
+__device__ __forceinline__ uint32_t ctr_read(const unsigned int* a) { return FRESH ? __ldcg(a) : *a; }
+
 // huge cells i0, i0 + stride, ...
-// (the run counters that the passes read are read past L1: in a one-launch
-// query they change between phases of the same kernel)
+template <bool FRESH = false>
 __device__ __forceinline__ void expand_cells(const Params& p, uint32_t i0, uint32_t stride) {
-    const uint32_t nh = mn64(__ldcg(&p.ctr->n_list[kListHuge]), p.list_cap[kListHuge]);
+    const uint32_t nh = mn64(ctr_read<FRESH>(&p.ctr->n_list[kListHuge]), p.list_cap[kListHuge]);
     for (uint32_t i = i0; i < nh; i += stride) {
         const uint2 sn = p.lists[p.list_off[kListHuge] + i];
         const uint32_t n = sn.y;
@@ -1240,12 +1246,12 @@ __device__ __forceinline__ void small_sweep(const Params& p, const Slots& s, War
     }
 }
 
-template <int D, int WG, bool BIP, bool NARROW, bool REC>
+template <int D, int WG, bool BIP, bool NARROW, bool REC, bool FRESH = false>
 __device__ __forceinline__ void small_items(const Params& p, const Slots& s, WarpOut& o, int list, uint64_t first,
                                             uint64_t stride) {
     constexpr uint32_t G = 32 / WG;
     const uint32_t lane = lane_id(), g = lane / WG, r = lane % WG;
-    const uint64_t nl = mn64(__ldcg(&p.ctr->n_list[list]), p.list_cap[list]);
+    const uint64_t nl = mn64(ctr_read<FRESH>(&p.ctr->n_list[list]), p.list_cap[list]);
     const uint64_t nitems = (nl + G - 1) / G;
     for (uint64_t item = first; item < nitems; item += stride) {
         uint32_t n1, gid;
@@ -1262,16 +1268,16 @@ __device__ __forceinline__ void rec_hits(const Params& p, const WarpOut& o) {
 
 // the four small-cell lists, warp gw of nw; per-warp staging in s_a, s_b
 // (kSmallSlots each) and an output buffer of kWarpOut pairs
-template <int D, bool BIP, bool NARROW, bool REC>
+template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false>
 __device__ __forceinline__ void small_pass(const Params& p, uint4* s_a, uint4* s_b, uint2* s_out, uint64_t gw,
                                            uint64_t nw) {
     const Slots s{s_a, s_b};
     WarpOut o{s_out, 0, kWarpOut};
     // classes interleaved over the warps so every warp gets a similar mix
-    small_items<D, 32, BIP, NARROW, REC>(p, s, o, 3, gw, nw);
-    small_items<D, 16, BIP, NARROW, REC>(p, s, o, 2, (gw + nw / 4) % nw, nw);
-    small_items<D, 8, BIP, NARROW, REC>(p, s, o, 1, (gw + nw / 2) % nw, nw);
-    small_items<D, 4, BIP, NARROW, REC>(p, s, o, 0, (gw + 3 * nw / 4) % nw, nw);
+    small_items<D, 32, BIP, NARROW, REC, FRESH>(p, s, o, 3, gw, nw);
+    small_items<D, 16, BIP, NARROW, REC, FRESH>(p, s, o, 2, (gw + nw / 4) % nw, nw);
+    small_items<D, 8, BIP, NARROW, REC, FRESH>(p, s, o, 1, (gw + nw / 2) % nw, nw);
+    small_items<D, 4, BIP, NARROW, REC, FRESH>(p, s, o, 0, (gw + 3 * nw / 4) % nw, nw);
     wflush(p, o);
     if (REC) rec_hits(p, o);
 }
@@ -1441,13 +1447,13 @@ __device__ __forceinline__ uint32_t diag_allow(uint32_t allow, uint32_t lane, ui
 // shared memory (staging slots, then the output buffer)
 constexpr uint32_t kMedWarpBytes = kMedSlots * 2 * sizeof(uint4) + kMedOut * sizeof(uint2);
 
-template <int D, bool BIP, bool NARROW, bool REC>
+template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false>
 __device__ __forceinline__ void med_pass(const Params& p, unsigned char* wsm, uint64_t gw, uint64_t nw) {
     const uint32_t lane = lane_id();
     uint4* base = reinterpret_cast<uint4*>(wsm);
     const Slots s{base, base + kMedSlots};
     WarpOut o{reinterpret_cast<uint2*>(base + 2 * kMedSlots), 0, kMedOut};
-    const uint64_t nl = mn64(__ldcg(&p.ctr->n_list[kListMed]), p.list_cap[kListMed]);
+    const uint64_t nl = mn64(ctr_read<FRESH>(&p.ctr->n_list[kListMed]), p.list_cap[kListMed]);
     for (uint64_t item = gw; item < nl; item += nw) {
         const uint2 sn = p.lists[p.list_off[kListMed] + item];
         const uint32_t gid = sn.x;  // record mode: the cell id (its start is in the counters)
@@ -1639,12 +1645,12 @@ __device__ __forceinline__ void bremit(const Params& p, BlockSmem& s, uint32_t m
     if (wb) rec_write(dst + w + wa, keep, row, mb, lb);
 }
 
-template <int D, bool BIP, bool NARROW, bool REC>
+template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false>
 __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const Slots sl{s.a, s.b};
     auto emit = [&](uint32_t ma, auto pa, uint32_t mb, auto pb, uint32_t myid) { bemit<BIP>(p, s, ma, pa, mb, pb, myid); };
-    const uint64_t nl = mn64(__ldcg(&p.ctr->n_list[kListBig]), p.list_cap[kListBig]);
+    const uint64_t nl = mn64(ctr_read<FRESH>(&p.ctr->n_list[kListBig]), p.list_cap[kListBig]);
     uint64_t cur = task * kBigCellsPerTask;
     const uint64_t end = mn64(cur + kBigCellsPerTask, nl);
     while (cur < end) {
@@ -1721,11 +1727,11 @@ __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
 
 // huge cells: one tile task {start, n, r, x0} per warp; boxes gathered per
 // tile into the warp's 64 slots (32 rows, 32 columns)
-template <int D, bool BIP, bool NARROW, bool REC>
+template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false>
 __device__ __forceinline__ void huge_item(const Params& p, BlockSmem& s, uint64_t item, uint32_t slot0) {
     const uint32_t lane = lane_id();
     const Slots sl{s.a, s.b};
-    const uint64_t nt = mn64(__ldcg(&p.ctr->need_tasks), p.task_cap);
+    const uint64_t nt = mn64(ctr_read<FRESH>(&p.ctr->need_tasks), p.task_cap);
     if (item >= nt) return;
     const uint4 tk = p.tasks[item];
     const uint32_t gid = tk.x;  // record mode: the cell id; its start is in the counters
@@ -1779,23 +1785,23 @@ __device__ __forceinline__ void huge_item(const Params& p, BlockSmem& s, uint64_
 }
 
 // big-cell tasks and huge-cell tile tasks, block blk of nblk
-template <int D, bool BIP, bool NARROW, bool REC>
+template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false>
 __device__ __forceinline__ void block_pass(const Params& p, BlockSmem& s, uint64_t blk, uint64_t nblk) {
     const uint32_t t = threadIdx.x, warp = t >> 5;
     if (t == 0) {
         s.out_n = 0;
         s.first_ovf = kBlockOut;
         s.hits = 0;
-        const uint64_t nb = mn64(__ldcg(&p.ctr->n_list[kListBig]), p.list_cap[kListBig]);
-        const uint64_t nt = mn64(__ldcg(&p.ctr->need_tasks), p.task_cap);
+        const uint64_t nb = mn64(ctr_read<FRESH>(&p.ctr->n_list[kListBig]), p.list_cap[kListBig]);
+        const uint64_t nt = mn64(ctr_read<FRESH>(&p.ctr->need_tasks), p.task_cap);
         s.nbt[0] = (nb + kBigCellsPerTask - 1) / kBigCellsPerTask;
         s.nbt[1] = (nt + kPairWarps - 1) / kPairWarps;
     }
     __syncthreads();
     const uint64_t total = s.nbt[0] + s.nbt[1];
     for (uint64_t bt = blk; bt < total; bt += nblk) {
-        if (bt < s.nbt[0]) big_task<D, BIP, NARROW, REC>(p, s, bt);
-        else huge_item<D, BIP, NARROW, REC>(p, s, (bt - s.nbt[0]) * kPairWarps + warp, warp * 64);
+        if (bt < s.nbt[0]) big_task<D, BIP, NARROW, REC, FRESH>(p, s, bt);
+        else huge_item<D, BIP, NARROW, REC, FRESH>(p, s, (bt - s.nbt[0]) * kPairWarps + warp, warp * 64);
         __syncthreads();
         const uint32_t on = s.out_n, ovf = s.first_ovf;
         const uint32_t nv = min(on, ovf);
@@ -2194,7 +2200,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArg
     FUSED_BARRIER()
     // P3: tile tasks of huge cells, scatter (against the cell ends)
     if (fits) {
-        expand_cells(p, (uint32_t)gt, (uint32_t)nt);
+        expand_cells<true>(p, (uint32_t)gt, (uint32_t)nt);
         Params pe = p;
         if (p.ncells <= kFusedLocalCells) pe.counts = a.ends;
         box_pass<D, true, false>(pe, sbox, blk, nblk);
@@ -2211,12 +2217,12 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArg
     if (fits) {
         unsigned char* ws = smem_raw + warp * kSmallWarpBytes;
         uint4* sa = reinterpret_cast<uint4*>(ws);
-        small_pass<D, false, NARROW, false>(p, sa, sa + kSmallSlots, reinterpret_cast<uint2*>(sa + 2 * kSmallSlots),
+        small_pass<D, false, NARROW, false, true>(p, sa, sa + kSmallSlots, reinterpret_cast<uint2*>(sa + 2 * kSmallSlots),
                                             gw, nw);
         __syncthreads();
-        med_pass<D, false, NARROW, false>(p, smem_raw + warp * kMedWarpBytes, gw, nw);
+        med_pass<D, false, NARROW, false, true>(p, smem_raw + warp * kMedWarpBytes, gw, nw);
         __syncthreads();
-        block_pass<D, false, NARROW, false>(p, *reinterpret_cast<BlockSmem*>(smem_raw), blk, nblk);
+        block_pass<D, false, NARROW, false, true>(p, *reinterpret_cast<BlockSmem*>(smem_raw), blk, nblk);
     }
     // the last block to finish copies the run counters to the host (one
     // more arrival per block on the barriers' count)

@@ -112,6 +112,9 @@ def lib():
     return _LIB
 
 
+_LEGACY_STREAM = 0x1  # cudaStreamLegacy
+
+
 def _check(rc: int, allow=(OK,)) -> int:
     if rc not in allow:
         raise PbigError(rc, lib().pbig2_last_error().decode())
@@ -175,9 +178,14 @@ class Engine:
 
     @staticmethod
     def _stream(stream):
+        """None: the context's own stream. A torch stream or a raw handle
+        otherwise; torch's default stream (handle 0) becomes CUDA's legacy
+        default stream, so the query is ordered with torch's work on it (a
+        null handle would select the context's own non-blocking stream)."""
         if stream is None:
             return None
-        return C.c_void_p(getattr(stream, "cuda_stream", stream))
+        h = getattr(stream, "cuda_stream", stream)
+        return C.c_void_p(h if h else _LEGACY_STREAM)
 
     def self_intersect(self, boxes, range_: int, cell_shift: int | None = None, stream=None,
                        allow_bad: bool = False) -> int:

@@ -134,16 +134,18 @@ def test_bounded_barrier_wait_runs_out():
             assert np.array_equal(canon(e.pairs()), want)
 
 
-def test_back_to_back_behind_other_work(two):
-    """Launches queued behind other device work (a 256 MB memset each, no
-    host synchronisation in between) start their blocks at different times:
-    every result must still be exact. Config 1 (a 64 x 64 grid: each block
-    sums the chunks itself) and a clustered 3-D scene on 64 x 64 x 64 cells
-    (the chunk totals shared through a barrier)."""
+def test_back_to_back_beside_other_work(two):
+    """Launches on the context's own stream while torch's default stream
+    runs other device work (a 256 MB memset before each query, no host
+    synchronisation in between): the launch's blocks start at different
+    times as the other kernel leaves the SMs, and every result must still be
+    exact. Config 1 (a 64 x 64 grid: each block sums the chunks itself) and a
+    clustered 3-D scene on 64 x 64 x 64 cells (the chunk totals shared
+    through a barrier)."""
     import torch
     one, _ = two
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    st = torch.cuda.current_stream()
+    st = None  # the context's own stream, not ordered with torch's default stream
     b1 = gen.uniform2d(65536, seed=0)
     b3 = gen.clustered3d(100000, seed=4)
     for boxes, shift in ((b1, None), (b3, 18)):
