@@ -461,6 +461,7 @@ def run_gb300(args, rank, local, ws):
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": desc, "boxes": n, "pairs": P, "range": rng, "cell_shift": stats["cell_shift"],
                    "entries": stats["entries"], "cells": stats["cells"], "pair_tests": stats["pair_tests"],
+                   "class_map": hex(stats["class_map"]),
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "flushed between steps (256 MiB write)"},
         "pairs_per_s": P * args.steps * ws / t_step,
@@ -565,7 +566,8 @@ def run_batched(args, rank, local, ws):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_b * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"{count} independent 3D scenes, sizes log-uniform in [256, 262144] (total {n} boxes), uniform centres, sides U[0.5,2]*n^(-1/3)*0.5, seed 0; every scene's cell size tuned inside the call",
-                   "scenes": count, "boxes": n, "pairs": P, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "scenes": count, "boxes": n, "pairs": P, "class_map": hex(st["class_map"]),
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "inputs (4.3 GB) far larger than L2"},
         "pairs_per_s": P * ws / t_b,
         "scenes_per_s": count * ws / t_b,

@@ -82,6 +82,11 @@ typedef struct {
     uint64_t jobs;
     uint32_t max_cell;
     uint32_t merged_blocks;
+    /* the class map the query used (PBIG2_OPT_CLASS_MAP) and the merged
+     * mode's block limit (PBIG2_OPT_MERGE_LIMIT) */
+    uint64_t class_map;
+    uint32_t merge_limit;
+    uint32_t pad;
 } pbig2_stats;
 
 /* Context: one device, owns its buffers and streams. Not thread-safe; use
@@ -225,6 +230,29 @@ PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
    one-launch query no barrier completes, every block gives up after about a
    second and the query returns PBIG2_ETIMEOUT; later queries run normally. */
 #define PBIG2_OPT_ONE_LAUNCH 5
+/* PBIG2_OPT_CLASS_MAP (default 0 = automatic): which pair kernel takes a cell
+   of n boxes. Nibble L (L = ceil(log2 n), 1..15; 15 also for larger cells)
+   names the list: 0..3 lane groups of 4, 8, 16, 32 lanes (cells up to that
+   many boxes), 4 one warp per cell staged whole (up to 128), 5 one block per
+   cell (up to 512), 6 tile tasks (any size; required for L = 15). A map that
+   sends a bucket to a list too small for it is refused. */
+#define PBIG2_OPT_CLASS_MAP 6
+/* PBIG2_OPT_MERGE_LIMIT (default 256, the reference's NTPB): merged mode's
+   block limit -- a block grows while its boxes stay within the limit. The
+   pair set does not depend on it; the merged build's statistics do. */
+#define PBIG2_OPT_MERGE_LIMIT 7
+
+/* The automatic class map: the work lists a query takes when no map is set
+   (one_launch: a small scene's one-launch query). Measured on GB300: the
+   default map (each cell to the smallest list that holds it) is the fastest
+   on the clustered 4M-box, red/blue and 4096-scene workloads; in a one-launch
+   query cells of 17..32 boxes go to the one-warp-per-cell pass instead (all
+   passes run at eight warps per SM there, and that pass tests faster). No
+   counterpart in the reference: its cell classes are fixed at build time. */
+PBIG2_API uint64_t pbig2_class_map_auto(uint32_t one_launch);
+/* 0 when every bucket of the class map names a list that can hold its cells,
+   else the first bucket that does not. */
+PBIG2_API uint32_t pbig2_class_map_check(uint64_t map);
 PBIG2_API int pbig2_set_option(pbig2_ctx* ctx, int option, int64_t value);
 
 /* One batch of the serving loop (no counterpart in the reference; the

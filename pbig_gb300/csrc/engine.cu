@@ -231,11 +231,12 @@ static int ensure_query_buffers(pbig2_ctx* c, Params& p, uint64_t entry_cap, uin
     // list regions: a cell of class c holds at least lo_c boxes, so with
     // E <= entry capacity no list can overflow
     const uint64_t ecap = c->d_entries.bytes / 4;
-    const uint64_t lo[kNumLists] = {2, 5, 9, 17, 33, kMedMax + 1, kBigMax + 1};
+    const unsigned long long map = p.class_map ? p.class_map : kClassMapDefault;
     uint64_t loff = 0;
     for (int k = 0; k < kNumLists; k++) {
+        const uint64_t lo = class_map_min(map, k);  // 0: the map sends no cell there
         p.list_off[k] = loff;
-        p.list_cap[k] = ecap / lo[k] + 1;
+        p.list_cap[k] = lo ? ecap / lo + 1 : 1;
         loff += p.list_cap[k];
     }
     CK(c->d_lists.ensure(loff * 8, false, st));
@@ -360,6 +361,7 @@ static int finish_query(pbig2_ctx* c, const Ctr& h, uint64_t nboxes, uint64_t nc
     s.jobs = h.jobs;
     s.max_cell = h.max_cell ? h.max_cell : (h.entries ? 1u : 0u);
     s.merged_blocks = c->merged_blocks;
+    s.merge_limit = c->merge_limit;
     s.pairs = c->npairs;
     s.cell_shift = scenes.empty() ? 0 : scenes[0].shift;
     s.scenes = nsc;
@@ -411,6 +413,7 @@ static int capture_graph(pbig2_ctx* c, const Params& p0, const uint32_t* d_boxes
     G.nscenes_cap = nsc;
     G.entry_cap = p.entry_cap;
     G.out_cap = p.out_cap;
+    G.class_map = c->class_map;  // the option (0: automatic), as graph_fits compares it
     G.launches = 13;  // scene table, count (2), scan (2), expand, scatter, pairs (3), scene grouping (3)
     G.buffers = c->buffers_sig();
     return PBIG2_OK;
@@ -423,9 +426,10 @@ static int capture_graph(pbig2_ctx* c, const Params& p0, const uint32_t* d_boxes
 // the first pass's per-cell counts) stays <= 256. merged[c] = the block root
 // of every cell of a block of two or more cells (the root included), else
 // kUnmerged. Returns the number of such blocks.
-static uint32_t merge_cells(std::vector<uint32_t>& nrs, std::vector<uint32_t>& merged, uint32_t nrc, int dims) {
+static uint32_t merge_cells(std::vector<uint32_t>& nrs, std::vector<uint32_t>& merged, uint32_t nrc, int dims,
+                            uint32_t limit) {
     const uint64_t C = nrs.size();
-    const uint32_t kLimit = 256;  // NTPB of the shipped build
+    const uint64_t kLimit = limit;  // NTPB of the shipped build by default (256)
     merged.assign(C, kUnmerged);
     const uint64_t nrc2 = (uint64_t)nrc * nrc;
     uint32_t blocks = 0;
@@ -521,7 +525,8 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     pbig2_ctx::Graph& G = c->graph;
     const bool graph_fits = c->use_graph && grouped && G.exec && G.boxes == d_boxes && G.dims == dims &&
                             G.range == range && G.split == split && nboxes <= G.nboxes_cap &&
-                            ncells <= G.ncells_cap && nsc <= G.nscenes_cap && G.buffers == c->buffers_sig();
+                            ncells <= G.ncells_cap && nsc <= G.nscenes_cap && G.buffers == c->buffers_sig() &&
+                            G.class_map == c->class_map;
 
     // tables -> pinned staging -> device (before the pipeline or graph)
     const size_t tab_bytes = nsc * sizeof(Scene), off_bytes = (nsc + 1) * sizeof(uint32_t);
@@ -567,7 +572,9 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
             c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
             est_entries = std::max(est_entries, (double)h.entries * 1.1);
         } else {
-            return finish_query(c, h, nboxes, ncells, nsc, scenes, grouped, launches, st);
+            const int rf = finish_query(c, h, nboxes, ncells, nsc, scenes, grouped, launches, st);
+            c->stats.class_map = c->class_map ? c->class_map : kClassMapDefault;
+            return rf;
         }
     }
 
@@ -605,6 +612,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     p.tile_state = c->d_state.as<unsigned long long>();
     p.ctr = c->d_ctr.as<Ctr>();
     p.dyn = nullptr;
+    p.class_map = c->class_map ? c->class_map : kClassMapDefault;
     c->merged_blocks = 0;
     bool one_grid = true;  // a single scene, or red and blue sharing one grid
     for (uint32_t i = 0; i < nsc; i++) one_grid = one_grid && scenes[i].grid_of == 0;
@@ -618,7 +626,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
         std::vector<uint32_t> nrs(ncells), merged;
         CK(cudaMemcpyAsync(nrs.data(), p0.counts, ncells * 4, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        c->merged_blocks = merge_cells(nrs, merged, tab[0].nrc, dims);
+        c->merged_blocks = merge_cells(nrs, merged, tab[0].nrc, dims, c->merge_limit);
         CK(c->d_merged.ensure(ncells * 4, false, st));
         CK(cudaMemcpyAsync(c->d_merged.p, merged.data(), ncells * 4, cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));  // `merged` goes out of scope
@@ -685,6 +693,7 @@ static int run_pipeline(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t nboxes, 
     if (h.err & (kErrEntryOvf | kErrTaskOvf | kErrOutOvf)) return fail(PBIG2_ENOMEM, "capacity retries exhausted");
     c->out_hint = std::max<uint64_t>(c->out_hint, h.pairs + h.pairs / 8);
     int rc = finish_query(c, h, nboxes, ncells, nsc, scenes, grouped, launches, st);
+    c->stats.class_map = p.class_map;
     if (rc != PBIG2_OK && rc != PBIG2_EINPUT) return rc;
     // capture this query's pipeline for later batches of the same shape
     if (G.exec && G.buffers != c->buffers_sig()) c->drop_graph();
@@ -735,6 +744,7 @@ static int fused_query(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t n, int di
     p.split = kNoSplit;
     p.max_range = range;
     p.tile_state = c->d_state.as<unsigned long long>();
+    p.class_map = c->class_map ? c->class_map : kClassMapOneLaunch;
     int rc = ensure_query_buffers(c, p, entry_cap, use_ext ? 1 : out_cap, task_cap, 1, false, st);
     if (rc) return rc;
     p.ctr = slots + c->fused_slot;
@@ -791,6 +801,7 @@ static int fused_query(pbig2_ctx* c, const uint32_t* d_boxes, uint64_t n, int di
     c->merged_blocks = 0;
     std::vector<GridScene> sc{{0, n, h.shift, 0}};
     rc = finish_query(c, h, n, h.cells, 1, sc, false, 1, st, false);
+    c->stats.class_map = p.class_map;
     c->stats.device_ms = h.t_end > h.t_start ? (double)(h.t_end - h.t_start) * 1e-6 : 0.0;  // the kernel's own clock
     return rc;
 }
@@ -895,6 +906,12 @@ PBIG2_API int pbig2_destroy(pbig2_ctx* c) {
     delete c;
     return PBIG2_OK;
 }
+
+PBIG2_API uint64_t pbig2_class_map_auto(uint32_t one_launch) {
+    return one_launch ? kClassMapOneLaunch : kClassMapDefault;
+}
+
+PBIG2_API uint32_t pbig2_class_map_check(uint64_t map) { return class_map_check(map); }
 
 PBIG2_API uint64_t pbig2_grid_cells(uint32_t range, uint32_t shift, uint32_t dims) {
     return grid_cells(range, shift, (int)dims);
@@ -1322,6 +1339,22 @@ PBIG2_API int pbig2_set_option(pbig2_ctx* c, int option, int64_t value) {
     }
     if (option == PBIG2_OPT_RICE) {
         c->rice_mode = value != 0;
+        return PBIG2_OK;
+    }
+    if (option == PBIG2_OPT_CLASS_MAP) {
+        const unsigned long long map = (unsigned long long)value;
+        if (map) {
+            const uint32_t bad = class_map_check(map);
+            if (bad)
+                return fail(PBIG2_EINVAL, "class map 0x%llx: bucket %u names a list that cannot hold its cells", map,
+                            bad);
+        }
+        c->class_map = map;
+        return PBIG2_OK;
+    }
+    if (option == PBIG2_OPT_MERGE_LIMIT) {
+        if (value < 0 || value > (1 << 30)) return fail(PBIG2_EINVAL, "merge limit %lld", (long long)value);
+        c->merge_limit = value ? (uint32_t)value : 256u;
         return PBIG2_OK;
     }
     if (option == PBIG2_OPT_ONE_LAUNCH) {

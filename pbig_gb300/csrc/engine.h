@@ -94,6 +94,7 @@ struct pbig2_ctx {
         int dims = 0;
         uint32_t range = 0, split = 0;
         uint64_t nboxes_cap = 0, ncells_cap = 0, nscenes_cap = 0, entry_cap = 0, out_cap = 0;
+        unsigned long long class_map = 0;
         uintptr_t buffers = 0;  // buffers_sig() at capture: any reallocation invalidates the graph
         int launches = 0;
     } graph;
@@ -119,6 +120,9 @@ struct pbig2_ctx {
     bool fused_dirty = true;     // the counters may hold values another pipeline left (or are new)
     uint64_t fused_entry_hint = 0;
     bool fused_stall_test = false;  // the next launch's barriers never complete (test of the bounded wait)
+    // work-list class map of later queries (PBIG2_OPT_CLASS_MAP; 0: automatic)
+    unsigned long long class_map = 0;
+    uint32_t merge_limit = 256;  // merged mode's block limit (PBIG2_OPT_MERGE_LIMIT)
     // autotuner memo: (n, dims, range, mean extent) -> shift
     struct TuneMemo { uint64_t n; int dims; uint32_t range; double ext; uint32_t shift; double est_e; };
     std::vector<TuneMemo> memo;

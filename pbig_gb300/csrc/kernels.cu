@@ -435,11 +435,11 @@ struct TileRec {                         // 64 bytes per tile
 };
 static_assert(sizeof(TileRec) == 64, "tile record layout");
 
-static_assert(kMedMax == 128 && kBigMax == 512, "list bounds are powers of two");
-constexpr unsigned long long kClassByLog = 0x6666665544321000ull;  // nibble L: list of ceil(log2 n) = L
-__device__ __forceinline__ uint32_t class_of(uint32_t n) {
+static_assert(kMedMax == 128 && kBigMax == 512, "list bounds are powers of two (the class map's buckets)");
+// the work list of a cell of n >= 2 boxes under the class map
+__device__ __forceinline__ uint32_t class_of(uint32_t n, unsigned long long map) {
     const uint32_t lg = 32u - __clz(n - 1u);  // ceil(log2 n) for n >= 2
-    return (uint32_t)(kClassByLog >> (4u * min(lg, 15u))) & 15u;
+    return (uint32_t)(map >> (4u * min(lg, 15u))) & 15u;
 }
 
 __device__ __forceinline__ unsigned long long warp_incl_scan64(unsigned long long v) {
@@ -616,6 +616,7 @@ __device__ __forceinline__ void scan_chunk(const Params& p, const Params& pl, ui
                                            const uint32_t (&v)[4 * Q], unsigned long long base, ScanStats& ws) {
     constexpr int kPer = 4 * Q;
     const uint32_t lane = lane_id();
+    const unsigned long long cmap = p.class_map ? p.class_map : kClassMapDefault;
     uint32_t big = 0;
 #pragma unroll
     for (int k = 0; k < kPer; k++) big |= v[k] >> 1;
@@ -651,7 +652,7 @@ __device__ __forceinline__ void scan_chunk(const Params& p, const Params& pl, ui
 #pragma unroll
         for (int k = 0; k < kPer; k++) {
             if (v[k] >= 2u) {
-                const uint32_t c = class_of(v[k]);
+                const uint32_t c = class_of(v[k], cmap);
                 if (c < 6u) pk += 1ull << (10u * c);
                 else pk6 += 1u;
             }
@@ -670,7 +671,7 @@ __device__ __forceinline__ void scan_chunk(const Params& p, const Params& pl, ui
         }
 #pragma unroll
         for (int k = 0; k < kPer; k++) {
-            const uint32_t c = v[k] >= 2u ? class_of(v[k]) : 0u;
+            const uint32_t c = v[k] >= 2u ? class_of(v[k], cmap) : 0u;
             const uint32_t b = __shfl_sync(FULL_MASK, lbase, c);
             if (v[k] >= 2u) {
                 uint32_t rk;

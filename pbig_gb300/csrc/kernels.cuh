@@ -33,6 +33,33 @@ constexpr int kListMed = 4, kListBig = 5, kListHuge = 6;
 constexpr uint32_t kMedMax = 128;   // largest cell staged by one warp
 constexpr uint32_t kBigMax = 512;   // largest cell staged by one block
 
+// Which list a cell goes to is a class map: nibble L (L = ceil(log2 n), 1..15;
+// 15 also for larger cells) holds the list of cells of n in (2^(L-1), 2^L].
+// A list takes cells up to its capacity: 4, 8, 16, 32 boxes (lists 0..3, a
+// lane group of that width per cell), kMedMax (4), kBigMax (5), any (6). The
+// default sends each bucket to the smallest list that holds it.
+constexpr unsigned long long kClassMapDefault = 0x6666665544321000ull;
+constexpr unsigned long long kClassMapOneLaunch = 0x6666665544421000ull;  // 17..32 to the one-warp pass
+__host__ __device__ inline uint32_t class_map_list(unsigned long long map, uint32_t L) {
+    return (uint32_t)(map >> (4u * (L < 15u ? L : 15u))) & 15u;
+}
+// 0 when every bucket L = 1..15 names a list that holds it, else the first bad bucket
+__host__ __device__ inline uint32_t class_map_check(unsigned long long map) {
+    const uint64_t cap[kNumLists] = {4, 8, 16, 32, kMedMax, kBigMax, ~0ull};
+    for (uint32_t L = 1; L <= 15; L++) {
+        const uint32_t k = class_map_list(map, L);
+        if (k >= (uint32_t)kNumLists || (L < 15 && (1ull << L) > cap[k]) || (L == 15 && k != (uint32_t)kListHuge))
+            return L;
+    }
+    return 0;
+}
+// smallest cell a list can receive under the map (0: none), for list capacities
+__host__ __device__ inline uint64_t class_map_min(unsigned long long map, int list) {
+    for (uint32_t L = 1; L <= 15; L++)
+        if (class_map_list(map, L) == (uint32_t)list) return L == 1 ? 2 : (1ull << (L - 1)) + 1;
+    return 0;
+}
+
 // cells of a dims-D grid with ceil(range / 2^shift) cells per axis,
 // saturating at UINT64_MAX (in 3-D a fine grid over a wide range has more
 // than 2^64 cells: range 2^32 at shift 0 gives 2^96)
@@ -163,6 +190,7 @@ struct Params {
     const uint32_t* merged;       // merged mode (one scene): cell -> root of its merged block, or kUnmerged
     uint32_t records;             // record mode: work lists hold {cell id, n}; the pair kernels write the
                                   // reference's Rice record stream (8-byte words) instead of pairs
+    unsigned long long class_map; // cell size -> work list (0: kClassMapDefault)
     // upload fused into the count: when box_copy is set, the count reads the
     // boxes from page-locked host memory (boxes [0, up_split) at up_red, the
     // rest at up_blue, device-mapped addresses) and writes them to box_copy,

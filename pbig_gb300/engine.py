@@ -32,7 +32,7 @@ EXPORTS = [
     "pbig2_noalloc_last_error", "pbig2_set_option", "pbig2_scene_create", "pbig2_scene_destroy",
     "pbig2_scene_move", "pbig2_scene_delta", "pbig2_scene_pairs", "pbig2_scene_boxes", "pbig2_scene_copy",
     "pbig2_result_records", "pbig2_copy_records", "pbig2_decode_records", "pbig2_serve_batch",
-    "pbig2_grid_cells", "pbig2_result_scene_shifts",
+    "pbig2_grid_cells", "pbig2_result_scene_shifts", "pbig2_class_map_auto", "pbig2_class_map_check",
 ]
 
 
@@ -54,7 +54,8 @@ class Stats(C.Structure):
                 ("cell_shift", C.c_uint32), ("scenes", C.c_uint32), ("kernels", C.c_uint32),
                 ("grid_retries", C.c_uint32), ("device_ms", C.c_double), ("phase_ms", C.c_double * 9),
                 ("comp_pairs", C.c_uint64), ("jobs", C.c_uint64), ("max_cell", C.c_uint32),
-                ("merged_blocks", C.c_uint32)]
+                ("merged_blocks", C.c_uint32), ("class_map", C.c_uint64), ("merge_limit", C.c_uint32),
+                ("pad", C.c_uint32)]
 
     PHASES = ("count", "scan", "expand", "scatter", "pairs", "group", "pairs_small", "pairs_med", "pairs_block")
 
@@ -103,6 +104,10 @@ def lib():
         L.pbig2_tune_shift.argtypes = [vp, u64, u32, u32, u64, C.POINTER(u32)]
         L.pbig2_grid_cells.argtypes = [u32, u32, u32]
         L.pbig2_grid_cells.restype = u64
+        L.pbig2_class_map_auto.argtypes = [u32]
+        L.pbig2_class_map_auto.restype = u64
+        L.pbig2_class_map_check.argtypes = [u64]
+        L.pbig2_class_map_check.restype = u32
         L.pbig2_self_intersect_noalloc.argtypes = [vp, u64, u32, u32, u32, vp, u64, C.POINTER(u64), vp]
         L.pbig2_noalloc_last_error.restype = C.c_char_p
         L.pbig2_set_option.argtypes = [vp, C.c_int, C.c_int64]
@@ -350,6 +355,15 @@ class Engine:
         """Run small self queries (at most 262 144 boxes) as one cooperative
         kernel launch (on by default); off: the regular pipeline."""
         _check(self._L.pbig2_set_option(self._ctx, 5, int(bool(on))))
+
+    def set_class_map(self, cmap: int) -> None:
+        """Which pair kernel takes a cell of n boxes (PBIG2_OPT_CLASS_MAP):
+        nibble ceil(log2 n) names the list; 0 restores the automatic choice."""
+        _check(self._L.pbig2_set_option(self._ctx, 6, int(cmap) - (1 << 64) if cmap >= 1 << 63 else int(cmap)))
+
+    def set_merge_limit(self, limit: int) -> None:
+        """Merged mode's block limit in boxes (PBIG2_OPT_MERGE_LIMIT; 0: 256)."""
+        _check(self._L.pbig2_set_option(self._ctx, 7, int(limit)))
 
     def set_graphs(self, on: bool) -> None:
         """Capture/replay batched queries as CUDA graphs (on by default)."""
