@@ -601,9 +601,11 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t pari
 }
 
 // the cells of chunk ch (counts v; `base` entries before the chunk): each
-// cell's end (start + count) into its counter, each cell of two or more boxes
-// into its work list (one atomic per list and chunk), and the work
-// statistics into ws
+// non-empty cell's end (start + count) into its counter (an empty cell's is
+// never read: the scatter and the work lists touch cells with entries only,
+// and skipping those stores, most of a fine grid, saves the scatter the
+// write-backs of their lines), each cell of two or more boxes into its work
+// list (one atomic per list and chunk), and the work statistics into ws
 struct ScanStats {
     unsigned long long tests = 0;
     uint32_t half = 0, jobs = 0, max = 0;
@@ -634,15 +636,16 @@ __device__ __forceinline__ void scan_chunk(const Params& p, const Params& pl, ui
             st[4 * q + k] = (uint32_t)run;
             run += v[4 * q + k];
         }
-        // the cell's counter becomes its end (start + count), in place
+        // a non-empty cell's counter becomes its end (start + count), in place
         const uint64_t c = chunk_cell<Q>(ch, q);
         if (full) {
-            *reinterpret_cast<uint4*>(p.counts + c) = make_uint4(
-                st[4 * q] + v[4 * q], st[4 * q + 1] + v[4 * q + 1], st[4 * q + 2] + v[4 * q + 2], st[4 * q + 3] + v[4 * q + 3]);
+            if (rs != 0u)
+                *reinterpret_cast<uint4*>(p.counts + c) = make_uint4(
+                    st[4 * q] + v[4 * q], st[4 * q + 1] + v[4 * q + 1], st[4 * q + 2] + v[4 * q + 2], st[4 * q + 3] + v[4 * q + 3]);
         } else {
 #pragma unroll
             for (int k = 0; k < 4; k++)
-                if (c + k < p.ncells) p.counts[c + k] = st[4 * q + k] + v[4 * q + k];
+                if (c + k < p.ncells && v[4 * q + k] != 0u) p.counts[c + k] = st[4 * q + k] + v[4 * q + k];
         }
     }
     if (__any_sync(FULL_MASK, big != 0)) {
