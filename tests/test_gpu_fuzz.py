@@ -55,17 +55,24 @@ def scene_params(seed):
 
 @pytest.mark.parametrize("seed", range(40))
 def test_random_self(engine, seed):
+    """Each scene through the one-launch path (these scenes are small) and
+    through the regular multi-launch pipeline."""
     rs, dims, rng, n = scene_params(seed)
     boxes = random_scene(rs, n, dims, rng)
     want = O.brute_pairs(boxes)
     top = max(1, int(rng - 1).bit_length())
     shifts = [None] + sorted(set(int(s) for s in rs.integers(max(0, top - 9), top + 1, size=2)))
-    for s in shifts:
-        if s is not None and (((rng + (1 << s) - 1) >> s) ** dims) > 1 << 25:
-            continue  # a box may cover fewer than 2^26 cells
-        got = engine.self_intersect(boxes, rng, cell_shift=s)
-        assert got == len(want), (seed, s)
-        assert np.array_equal(canon(engine.pairs()), want), (seed, s)
+    try:
+        for one_launch in (True, False):
+            engine.set_one_launch(one_launch)
+            for s in shifts:
+                if s is not None and (((rng + (1 << s) - 1) >> s) ** dims) > 1 << 25:
+                    continue  # a box may cover fewer than 2^26 cells
+                got = engine.self_intersect(boxes, rng, cell_shift=s)
+                assert got == len(want), (seed, s, one_launch)
+                assert np.array_equal(canon(engine.pairs()), want), (seed, s, one_launch)
+    finally:
+        engine.set_one_launch(True)
 
 
 @pytest.mark.parametrize("seed", range(12))
