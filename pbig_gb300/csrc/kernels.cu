@@ -369,11 +369,11 @@ __global__ void k_zero_counts(Params pin) {
     for (uint64_t i = 4 * n4 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.ncells; i += stride) p.counts[i] = 0;
 }
 
-// tiles of kBoxThreads boxes: blk, blk + nblk, ... (blockDim.x == kBoxThreads)
-template <int D, bool SCATTER, bool MERGED>
+// tiles of TILE boxes: blk, blk + nblk, ... (blockDim.x == TILE)
+template <int D, bool SCATTER, bool MERGED, uint32_t TILE = kBoxThreads>
 __device__ __forceinline__ void box_pass(const Params& p, uint32_t* sbox, uint64_t blk, uint64_t nblk) {
-    for (uint64_t b0 = blk * kBoxThreads; b0 < p.nboxes; b0 += nblk * kBoxThreads) {
-        const uint32_t nb = (uint32_t)mn64(kBoxThreads, p.nboxes - b0);
+    for (uint64_t b0 = blk * TILE; b0 < p.nboxes; b0 += nblk * TILE) {
+        const uint32_t nb = (uint32_t)mn64(TILE, p.nboxes - b0);
         if (!SCATTER && p.box_copy) stage_upload<D>(p, b0, nb, sbox);
         else stage_boxes<D>(p, b0, nb, sbox);
         __syncthreads();
@@ -1021,16 +1021,31 @@ __device__ __forceinline__ void wemit(const Params& p, WarpOut& o, uint32_t ma, 
         }
     }
     uint32_t w = incl - k;
-    auto put = [&](uint32_t q) {
+    auto pair = [&](uint32_t q) {
         uint2 pr = make_uint2(min(myid, q), max(myid, q));
         if (BIP) pr.y -= p.split;
-        if (!direct) {
-            o.buf[o.n + w] = pr;
-        } else {
-            const unsigned long long g = gbase + w;
-            if (g < p.out_cap) p.out[g] = pr;
-            else atomicOr(&p.ctr->err, kErrOutOvf);
+        return pr;
+    };
+    if (!direct) {  // (warp-uniform: the loops below carry no per-pair branch)
+        uint2* dst = o.buf + o.n + w;
+        while (ma) {
+            const uint32_t bit = 31u - __clz(ma);  // highest set bit first
+            ma ^= 1u << bit;
+            *dst++ = pair(pa(bit));
         }
+        while (mb) {
+            const uint32_t bit = 31u - __clz(mb);
+            mb ^= 1u << bit;
+            *dst++ = pair(pb(bit));
+        }
+        __syncwarp();
+        o.n += total;
+        return;
+    }
+    auto put = [&](uint32_t q) {
+        const unsigned long long g = gbase + w;
+        if (g < p.out_cap) p.out[g] = pair(q);
+        else atomicOr(&p.ctr->err, kErrOutOvf);
         w++;
     };
     while (ma) {
@@ -1044,7 +1059,6 @@ __device__ __forceinline__ void wemit(const Params& p, WarpOut& o, uint32_t ma, 
         put(pb(bit));
     }
     __syncwarp();
-    if (!direct) o.n += total;
 }
 
 // ---- record mode: the reference's Rice stream ------------------------------
@@ -1547,6 +1561,13 @@ __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
 }
 
 // ---- big cells (block staged) and huge cells (tiles) -----------------------
+// a barrier of the whole block, or (SUB) of its first kPairThreads threads
+template <bool SUB>
+__device__ __forceinline__ void block_sync() {
+    if constexpr (SUB) asm volatile("bar.sync 1, %0;" ::"n"(kPairThreads) : "memory");
+    else __syncthreads();
+}
+
 struct BlockSmem {
     uint4 a[kBlockSlots];
     uint4 b[kBlockSlots];
@@ -1649,7 +1670,7 @@ __device__ __forceinline__ void bremit(const Params& p, BlockSmem& s, uint32_t m
     if (wb) rec_write(dst + w + wa, keep, row, mb, lb);
 }
 
-template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false>
+template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false, bool SUB = false>
 __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const Slots sl{s.a, s.b};
@@ -1696,7 +1717,7 @@ __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
                 s.units = uinc;
             }
         }
-        __syncthreads();
+        block_sync<SUB>();
         const uint32_t K = s.k, tot = s.tot, U = s.units;
         if (K == 0) break;  // uniform: every thread read the same K
         for (uint32_t e = t; e < tot; e += kPairThreads) {
@@ -1708,7 +1729,7 @@ __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
             slot_put(sl, e, local < s.cell_n[c] ? load_box<D, NARROW>(p, p.entries[s.cell_start[c] + local])
                                                 : dummy_box<NARROW>());
         }
-        __syncthreads();
+        block_sync<SUB>();
         for (uint32_t u = warp; u < U; u += kPairWarps) {
             uint32_t c = 0;
 #pragma unroll
@@ -1724,7 +1745,7 @@ __device__ void big_task(const Params& p, BlockSmem& s, uint64_t task) {
                 row_unit<D, BIP, NARROW, false>(p, sl, s.cell_off[c], s.cell_n[c], u - s.unit_pref[c], emit);
             }
         }
-        __syncthreads();
+        block_sync<SUB>();
         cur += K;
     }
 }
@@ -1788,8 +1809,9 @@ __device__ __forceinline__ void huge_item(const Params& p, BlockSmem& s, uint64_
     }
 }
 
-// big-cell tasks and huge-cell tile tasks, block blk of nblk
-template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false>
+// big-cell tasks and huge-cell tile tasks, block blk of nblk (SUB: run by
+// the block's first kPairThreads threads alone)
+template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false, bool SUB = false>
 __device__ __forceinline__ void block_pass(const Params& p, BlockSmem& s, uint64_t blk, uint64_t nblk) {
     const uint32_t t = threadIdx.x, warp = t >> 5;
     if (t == 0) {
@@ -1801,25 +1823,25 @@ __device__ __forceinline__ void block_pass(const Params& p, BlockSmem& s, uint64
         s.nbt[0] = (nb + kBigCellsPerTask - 1) / kBigCellsPerTask;
         s.nbt[1] = (nt + kPairWarps - 1) / kPairWarps;
     }
-    __syncthreads();
+    block_sync<SUB>();
     const uint64_t total = s.nbt[0] + s.nbt[1];
     for (uint64_t bt = blk; bt < total; bt += nblk) {
-        if (bt < s.nbt[0]) big_task<D, BIP, NARROW, REC, FRESH>(p, s, bt);
+        if (bt < s.nbt[0]) big_task<D, BIP, NARROW, REC, FRESH, SUB>(p, s, bt);
         else huge_item<D, BIP, NARROW, REC, FRESH>(p, s, (bt - s.nbt[0]) * kPairWarps + warp, warp * 64);
-        __syncthreads();
+        block_sync<SUB>();
         const uint32_t on = s.out_n, ovf = s.first_ovf;
         const uint32_t nv = min(on, ovf);
         const bool last = bt + nblk >= total;
         if (nv >= kBlockOut / 2 || on > nv || (last && on > 0)) {
             if (t == 0) s.gbase = nv ? atomicAdd(&p.ctr->pairs, (unsigned long long)nv) : 0ull;
-            __syncthreads();
+            block_sync<SUB>();
             store_run(p, s.gbase, s.out, nv, t, kPairThreads);
-            __syncthreads();
+            block_sync<SUB>();
             if (t == 0) {
                 s.out_n = 0;
                 s.first_ovf = kBlockOut;
             }
-            __syncthreads();
+            block_sync<SUB>();
         }
     }
     if (REC && t == 0 && s.hits) atomicAdd(&p.ctr->rec_pairs, s.hits);
@@ -1953,12 +1975,12 @@ __global__ void __launch_bounds__(1024) k_scene_offsets(Params pin, const unsign
 // barrier's wait is bounded: a block that gives up sets kErrWait and leaves,
 // and the others give up at their next barrier.
 // ---------------------------------------------------------------------------
-constexpr uint32_t kFusedThreads = kPairThreads;
+constexpr uint32_t kFusedThreads = 2 * kPairThreads;
+constexpr uint32_t kFusedWarps = kFusedThreads / 32;
 constexpr uint32_t kFusedChunks = (uint32_t)(kFusedMaxCells / kScanChunk);
 constexpr uint32_t kFusedLocalCells = 8192;  // grids of up to 8192 cells: 128-cell chunks, totals per block
 constexpr uint32_t kGridWaitLimit = 1u << 20;  // polls of 64 ns or more: the wait ends after a second at most
 constexpr uint32_t kSmallWarpBytes = 2 * kSmallSlots * sizeof(uint4) + kWarpOut * sizeof(uint2);
-static_assert(kFusedThreads == kBoxThreads, "box tiles of one block");
 static_assert(kFusedChunks % kFusedThreads == 0, "chunk prefixes per thread");
 
 // barrier number k of this launch (k counts the barriers passed so far)
@@ -2065,11 +2087,11 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArg
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t s_shift;
     __shared__ Scene s_scene;
-    __shared__ unsigned long long s_wsum[kPairWarps];
+    __shared__ unsigned long long s_wsum[kFusedWarps];
     __shared__ uint32_t s_csum[kFusedLocalCells / 128];
     const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
     const uint64_t blk = blockIdx.x, nblk = gridDim.x;
-    const uint64_t gw = blk * kPairWarps + warp, nw = nblk * kPairWarps;
+    const uint64_t gw = blk * kFusedWarps + warp, nw = nblk * kFusedWarps;
     const uint64_t gt = blk * kFusedThreads + t, nt = nblk * kFusedThreads;
     const uint32_t range = p.max_range;
     uint32_t nbar = 0;
@@ -2109,7 +2131,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArg
     }
     // P1: count
     uint32_t* sbox = reinterpret_cast<uint32_t*>(smem_raw);
-    box_pass<D, false, false>(p, sbox, blk, nblk);
+    box_pass<D, false, false, kFusedThreads>(p, sbox, blk, nblk);
     FUSED_BARRIER()
     // P2: chunk entry totals and prefixes, then the cells
     uint32_t* pre = reinterpret_cast<uint32_t*>(smem_raw);
@@ -2117,7 +2139,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArg
     bool fits;
     if (p.ncells <= kFusedLocalCells) {
         const uint32_t nch = (uint32_t)((p.ncells + 127) / 128);
-        for (uint32_t ch = warp; ch < nch; ch += kPairWarps) {
+        for (uint32_t ch = warp; ch < nch; ch += kFusedWarps) {
             uint32_t v[4];
             scan_load<1, true>(p, ch, v);
             s_csum[ch] = __reduce_add_sync(FULL_MASK, v[0] + v[1] + v[2] + v[3]);  // < 2^32 (at most 2^25)
@@ -2174,7 +2196,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArg
         __syncthreads();
         unsigned long long run = incl - sum;
 #pragma unroll
-        for (uint32_t w = 0; w < kPairWarps; w++) {
+        for (uint32_t w = 0; w < kFusedWarps; w++) {
             if (w < warp) run += s_wsum[w];
             total += s_wsum[w];
         }
@@ -2207,7 +2229,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArg
         expand_cells<true>(p, (uint32_t)gt, (uint32_t)nt);
         Params pe = p;
         if (p.ncells <= kFusedLocalCells) pe.counts = a.ends;
-        box_pass<D, true, false>(pe, sbox, blk, nblk);
+        box_pass<D, true, false, kFusedThreads>(pe, sbox, blk, nblk);
     }
     FUSED_BARRIER()
 #undef FUSED_BARRIER
@@ -2226,7 +2248,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArg
         __syncthreads();
         med_pass<D, false, NARROW, false, true>(p, smem_raw + warp * kMedWarpBytes, gw, nw);
         __syncthreads();
-        block_pass<D, false, NARROW, false, true>(p, *reinterpret_cast<BlockSmem*>(smem_raw), blk, nblk);
+        if (t < kPairThreads)  // (the block pass is laid out for kPairThreads threads)
+            block_pass<D, false, NARROW, false, true, true>(p, *reinterpret_cast<BlockSmem*>(smem_raw), blk, nblk);
     }
     // the last block to finish copies the run counters to the host (one
     // more arrival per block on the barriers' count)
@@ -2277,11 +2300,11 @@ static cudaError_t init_variant() {
 static int g_fused_blocks = 0;
 
 static size_t fused_smem() {
-    size_t b = (size_t)kPairWarps * kMedWarpBytes;
+    size_t b = (size_t)kFusedWarps * kMedWarpBytes;
     b = b > sizeof(BlockSmem) ? b : sizeof(BlockSmem);
-    b = b > (size_t)kPairWarps * kSmallWarpBytes ? b : (size_t)kPairWarps * kSmallWarpBytes;
+    b = b > (size_t)kFusedWarps * kSmallWarpBytes ? b : (size_t)kFusedWarps * kSmallWarpBytes;
     b = b > (size_t)kFusedChunks * 4 ? b : (size_t)kFusedChunks * 4;
-    b = b > (size_t)kBoxThreads * 7 * 4 ? b : (size_t)kBoxThreads * 7 * 4;
+    b = b > (size_t)kFusedThreads * 7 * 4 ? b : (size_t)kFusedThreads * 7 * 4;
     return b;
 }
 
