@@ -82,8 +82,61 @@ def cpu_sample(boxes, m: int):
     return np.ascontiguousarray(u)
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes (the driver's libnvidia-ml):
+    SM clock, its maximum, power and the active clock-event reasons of one
+    device. None when the library or the device cannot be opened."""
+
+    SM = 1  # NVML_CLOCK_SM
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    @classmethod
+    def open(cls, gpu: int):
+        import ctypes as C
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return None
+            h = C.c_void_p()
+            uuid = None
+            try:
+                import torch
+                uuid = getattr(torch.cuda.get_device_properties(gpu), "uuid", None)
+            except Exception:
+                uuid = None
+            rc = 1
+            if uuid is not None:
+                rc = lib.nvmlDeviceGetHandleByUUID(("GPU-" + str(uuid)).encode(), C.byref(h))
+            if rc != 0:
+                rc = lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(gpu), C.byref(h))
+            if rc != 0:
+                return None
+            reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+            if reasons is None:
+                reasons = lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            self = cls()
+            self.C, self.lib, self.h, self.reasons = C, lib, h, reasons
+            mx = C.c_uint()
+            self.max_mhz = float(mx.value) if lib.nvmlDeviceGetMaxClockInfo(h, cls.SM, C.byref(mx)) == 0 else None
+            return self
+        except Exception:
+            return None
+
+    def sample(self):
+        C = self.C
+        clk, pw, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, self.SM, C.byref(clk)) != 0:
+            return None
+        self.lib.nvmlDeviceGetPowerUsage(self.h, C.byref(pw))
+        active = self.reasons(self.h, C.byref(rs)) == 0
+        names = [nm for bit, nm in self.REASONS.items() if active and (rs.value & bit)]
+        return float(clk.value), pw.value / 1000.0, names
+
+
 class ClockSampler:
-    """nvidia-smi clocks/throttle sampling during the timed region."""
+    """Clocks and throttle reasons sampled during the timed region: NVML
+    queries every 5 ms (read-only), else nvidia-smi every 200 ms."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -92,11 +145,22 @@ class ClockSampler:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.rows = []
+        self.nvml_rows = []
         self._stop = threading.Event()
         self._t = None
+        self._nvml = _Nvml.open(gpu)
 
     def _run(self):
         while not self._stop.is_set():
+            if self._nvml is not None:
+                try:
+                    r = self._nvml.sample()
+                    if r is not None:
+                        self.nvml_rows.append(r)
+                except Exception:
+                    self._nvml = None
+                self._stop.wait(0.005)
+                continue
             try:
                 out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
                                       "--format=csv,noheader,nounits"], capture_output=True, text=True,
@@ -117,6 +181,11 @@ class ClockSampler:
         self._t.join(timeout=10)
 
     def summary(self):
+        if self.nvml_rows:
+            sm = [r[0] for r in self.nvml_rows]
+            reasons = sorted({nm for r in self.nvml_rows for nm in r[2]})
+            return {"sm_mhz": float(np.median(sm)), "sm_min_mhz": min(sm), "sm_max_mhz": self._nvml_max(),
+                    "reasons": reasons, "samples": len(self.nvml_rows), "source": "nvml, 5 ms"}
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
         sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
@@ -128,7 +197,11 @@ class ClockSampler:
                 if len(r) > 5 + k and r[5 + k].lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.rows)}
+                "reasons": sorted(reasons), "samples": len(self.rows), "source": "nvidia-smi, 200 ms"}
+
+    def _nvml_max(self):
+        n = self._nvml
+        return n.max_mhz if n is not None else None
 
 
 def algorithmic_bytes(st: dict, n: int) -> dict:
