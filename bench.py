@@ -136,14 +136,15 @@ class _Nvml:
 
 class ClockSampler:
     """Clocks and throttle reasons sampled during the timed region: NVML
-    queries every 5 ms (read-only), else nvidia-smi every 200 ms."""
+    queries every `period` seconds (read-only), else nvidia-smi every 200 ms."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu: int):
+    def __init__(self, gpu: int, period: float = 0.002):
         self.gpu = gpu
+        self.period = period
         self.rows = []
         self.nvml_rows = []
         self._stop = threading.Event()
@@ -159,7 +160,7 @@ class ClockSampler:
                         self.nvml_rows.append(r)
                 except Exception:
                     self._nvml = None
-                self._stop.wait(0.005)
+                self._stop.wait(self.period)
                 continue
             try:
                 out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
@@ -169,7 +170,7 @@ class ClockSampler:
                     self.rows.append([x.strip() for x in out.split(",")])
             except Exception:
                 pass
-            self._stop.wait(0.2)
+            self._stop.wait(max(self.period, 0.2))
 
     def __enter__(self):
         self._t = threading.Thread(target=self._run, daemon=True)
@@ -185,7 +186,7 @@ class ClockSampler:
             sm = [r[0] for r in self.nvml_rows]
             reasons = sorted({nm for r in self.nvml_rows for nm in r[2]})
             return {"sm_mhz": float(np.median(sm)), "sm_min_mhz": min(sm), "sm_max_mhz": self._nvml_max(),
-                    "reasons": reasons, "samples": len(self.nvml_rows), "source": "nvml, 5 ms"}
+                    "reasons": reasons, "samples": len(self.nvml_rows), "source": f"nvml, {self.period * 1e3:g} ms"}
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
         sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
@@ -763,7 +764,7 @@ def run_serving(args, rank, local, ws):
     # pairs are delivered into each slot's page-locked host buffer (the
     # device->host copy is timed; no second host copy)
     srv = serve.Server(device=local, budget_bytes=40 << 30, copy_pairs=False, reserve_boxes=4 << 20)
-    with ClockSampler(local) as clk:
+    with ClockSampler(local, period=0.05) as clk:  # (the serving loop runs in Python threads)
         th = serve.feed(srv, reqs)
         srv.serve(len(reqs))
         th.join()
