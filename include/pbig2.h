@@ -246,8 +246,9 @@ PBIG2_API int pbig2_get_stats(pbig2_ctx* ctx, pbig2_stats* stats);
    (one_launch: a small scene's one-launch query). Measured on GB300: the
    default map (each cell to the smallest list that holds it) is the fastest
    on the clustered 4M-box, red/blue and 4096-scene workloads; in a one-launch
-   query cells of 17..32 boxes go to the one-warp-per-cell pass instead (all
-   passes run at eight warps per SM there, and that pass tests faster). No
+   query cells of 5..32 boxes go to the one-warp-per-cell pass instead (all
+   passes run at one block per SM there, and a warp per cell keeps more
+   independent load chains in flight). No
    counterpart in the reference: its cell classes are fixed at build time. */
 PBIG2_API uint64_t pbig2_class_map_auto(uint32_t one_launch);
 /* 0 when every bucket of the class map names a list that can hold its cells,

@@ -39,7 +39,7 @@ constexpr uint32_t kBigMax = 512;   // largest cell staged by one block
 // lane group of that width per cell), kMedMax (4), kBigMax (5), any (6). The
 // default sends each bucket to the smallest list that holds it.
 constexpr unsigned long long kClassMapDefault = 0x6666665544321000ull;
-constexpr unsigned long long kClassMapOneLaunch = 0x6666665544421000ull;  // 17..32 to the one-warp pass
+constexpr unsigned long long kClassMapOneLaunch = 0x6666665544444000ull;  // 5..32 to the one-warp pass
 __host__ __device__ inline uint32_t class_map_list(unsigned long long map, uint32_t L) {
     return (uint32_t)(map >> (4u * (L < 15u ? L : 15u))) & 15u;
 }

@@ -4,7 +4,7 @@ the maps the engine refuses."""
 from pbig_gb300 import engine
 
 DEFAULT = 0x6666665544321000
-ONE_LAUNCH = 0x6666665544421000
+ONE_LAUNCH = 0x6666665544444000
 
 
 def _nib(m, L):
@@ -16,8 +16,8 @@ def test_automatic_maps():
     assert f(0) == DEFAULT and f(1) == ONE_LAUNCH
     # default: each bucket to the smallest list that holds it
     assert [_nib(DEFAULT, L) for L in range(1, 16)] == [0, 0, 1, 2, 3, 4, 4, 5, 5, 6, 6, 6, 6, 6, 6]
-    # one launch: cells of 17..32 boxes (bucket 5) to the one-warp-per-cell list
-    assert [_nib(ONE_LAUNCH, L) for L in range(1, 16)] == [0, 0, 1, 2, 4, 4, 4, 5, 5, 6, 6, 6, 6, 6, 6]
+    # one launch: cells of 5..32 boxes (buckets 3..5) to the one-warp-per-cell list
+    assert [_nib(ONE_LAUNCH, L) for L in range(1, 16)] == [0, 0, 4, 4, 4, 4, 4, 5, 5, 6, 6, 6, 6, 6, 6]
 
 
 def test_map_check():

@@ -12,7 +12,8 @@ from pbig_gb300 import Engine, gen
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 
-MAPS = [0x6666665544421000,   # 17..32 to one warp per cell (the one-launch choice)
+MAPS = [0x6666665544421000,   # 17..32 to one warp per cell
+        0x6666665544444000,   # 5..32 to one warp per cell (the one-launch choice)
         0x6666665554321000,   # 65..128 to one block per cell
         0x6666665555321000,   # 33..128 to one block per cell
         0x6666665544331000,   # 9..16 in lane groups of 32
