@@ -292,6 +292,7 @@ static cudaError_t record_pipeline(pbig2_ctx* c, const Params& p, int dims, bool
         // keep the grid and lists; clear the pair count and error word
         R(cudaMemsetAsync(&p.ctr->pairs, 0, sizeof(unsigned long long), st));
         R(cudaMemsetAsync(&p.ctr->err, 0, sizeof(unsigned int), st));
+        R(cudaMemsetAsync(&p.ctr->med_next, 0, sizeof(unsigned int), st));
         R(cudaEventRecordWithFlags(c->evp[4], st, evf));
     }
     // pairs stored over the host link: the lighter pair kernels run beside

@@ -839,10 +839,10 @@ constexpr uint32_t kSmallSlots = 32;        // per-warp staging, small cells
 constexpr uint32_t kMedSlots = kMedMax;     // per-warp staging, medium cells
 constexpr uint32_t kBlockSlots = kBigMax;   // per-block staging, big cells
 constexpr uint32_t kBlockOut = 2048;        // per-block output buffer (pairs)
-// big cells per block task: one, so the few hundred big cells of a large
-// scene spread over all blocks (eight per task kept 60 of 304 blocks busy on
-// the clustered 4M-box scene: 0.060 -> 0.028 ms)
-constexpr uint32_t kBigCellsPerTask = 1;
+// big cells per block task: two, so the few hundred big cells of a large
+// scene spread over the blocks (eight per task kept 60 of 304 blocks busy on
+// the clustered 4M-box scene: 0.060 ms; one per task 0.028, two 0.024 ms)
+constexpr uint32_t kBigCellsPerTask = 2;
 
 struct Box {
     uint32_t x0, x1, y0, y1, z0, z1, f, id;  // f: axes where the box does not start in this cell, << 29
@@ -1475,12 +1475,12 @@ __device__ __forceinline__ void med_pass(const Params& p, unsigned char* wsm, ui
     const Slots s{base, base + kMedSlots};
     WarpOut o{reinterpret_cast<uint2*>(base + 2 * kMedSlots), 0, kMedOut};
     const uint64_t nl = mn64(ctr_read<FRESH>(&p.ctr->n_list[kListMed]), p.list_cap[kListMed]);
-    for (uint64_t item = gw; item < nl; item += nw) {
+    auto cell = [&](uint64_t item) {
         const uint2 sn = p.lists[p.list_off[kListMed] + item];
         const uint32_t gid = sn.x;  // record mode: the cell id (its start is in the counters)
         const uint32_t start = REC ? (gid < p.ncells ? p.counts[gid] : 0xffffffffu) : sn.x;
         const uint32_t n = sn.y;
-        if (n > kMedMax || (uint64_t)start + n > p.entry_cap) continue;  // inconsistent grid: skip
+        if (n > kMedMax || (uint64_t)start + n > p.entry_cap) return;  // inconsistent grid: skip
         const uint32_t R = (n + 31) >> 5;
         // stage: all entry ids first, then all boxes (loads in flight together)
         uint32_t raw[kMedSlots / 32];
@@ -1550,6 +1550,17 @@ __device__ __forceinline__ void med_pass(const Params& p, unsigned char* wsm, ui
             }
         }
         __syncwarp();
+    };
+    // items [0, nl - nl/4) in a fixed stride, the rest one at a time from a
+    // counter, so warps whose cells were larger end no later than the others
+    const uint64_t nfix = nl - nl / 4;
+    for (uint64_t item = gw; item < nfix; item += nw) cell(item);
+    for (;;) {
+        uint64_t item = 0;
+        if (lane == 0) item = nfix + atomicAdd(&p.ctr->med_next, 1u);
+        item = __shfl_sync(FULL_MASK, item, 0);
+        if (item >= nl) break;
+        cell(item);
     }
     wflush(p, o);
     if (REC) rec_hits(p, o);
