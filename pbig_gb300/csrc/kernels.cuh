@@ -143,7 +143,7 @@ struct Ctr {
     unsigned int n_tasks;               // tile tasks written for huge cells
     unsigned int need_tasks;            // tile tasks needed
     unsigned int max_cell;              // largest cell (or merged block) of two or more boxes
-    unsigned int med_next;              // medium-cell items taken one at a time (the last quarter)
+    unsigned int med_next;              // next medium-cell item (items are taken one at a time)
     unsigned long long entries;         // E
     unsigned long long pairs;           // pairs found (may exceed capacity)
     unsigned long long tests;           // sum of n(n-1)/2 over cells
