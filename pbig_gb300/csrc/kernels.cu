@@ -1464,13 +1464,14 @@ __device__ __forceinline__ uint32_t diag_allow(uint32_t allow, uint32_t lane, ui
     return a;
 }
 
-// the medium-cell list (every warp of the launch takes items from one
+// the medium-cell list, warp gw of nw (the one-launch kernel: items in a
+// fixed stride; the medium-cell kernel: every warp takes items from one
 // counter); wsm: the warp's kMedWarpBytes of shared memory (staging slots,
 // then the output buffer)
 constexpr uint32_t kMedWarpBytes = kMedSlots * 2 * sizeof(uint4) + kMedOut * sizeof(uint2);
 
 template <int D, bool BIP, bool NARROW, bool REC, bool FRESH = false>
-__device__ __forceinline__ void med_pass(const Params& p, unsigned char* wsm) {
+__device__ __forceinline__ void med_pass(const Params& p, unsigned char* wsm, uint64_t gw, uint64_t nw) {
     const uint32_t lane = lane_id();
     uint4* base = reinterpret_cast<uint4*>(wsm);
     const Slots s{base, base + kMedSlots};
@@ -1555,13 +1556,19 @@ __device__ __forceinline__ void med_pass(const Params& p, unsigned char* wsm) {
     // items taken one at a time from a counter, so warps whose cells were
     // larger end no later than the others (on the clustered 4M-box scene
     // 0.444 ms, against 0.499 ms for a fixed stride over the list and
-    // 0.455-0.50 ms for a fixed stride over its first half to seven eighths)
-    for (;;) {
-        uint64_t item = 0;
-        if (lane == 0) item = atomicAdd(&p.ctr->med_next, 1u);
-        item = __shfl_sync(FULL_MASK, item, 0);
-        if (item >= nl) break;
-        cell(item);
+    // 0.455-0.50 ms for a fixed stride over its first half to seven eighths).
+    // A one-launch query's warps take one or two cells each: there the
+    // counter's round trip costs more than the balance gains.
+    if constexpr (FRESH) {
+        for (uint64_t item = gw; item < nl; item += nw) cell(item);
+    } else {
+        for (;;) {
+            uint64_t item = 0;
+            if (lane == 0) item = atomicAdd(&p.ctr->med_next, 1u);
+            item = __shfl_sync(FULL_MASK, item, 0);
+            if (item >= nl) break;
+            cell(item);
+        }
     }
     wflush(p, o);
     if (REC) rec_hits(p, o);
@@ -1571,7 +1578,8 @@ template <int D, bool BIP, bool NARROW, bool REC = false>
 __global__ void __launch_bounds__(kPairThreads, 3) k_pairs_med(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t warp = threadIdx.x >> 5;
-    med_pass<D, BIP, NARROW, REC>(p, smem_raw + warp * kMedWarpBytes);
+    med_pass<D, BIP, NARROW, REC>(p, smem_raw + warp * kMedWarpBytes, (uint64_t)blockIdx.x * kPairWarps + warp,
+                                  (uint64_t)gridDim.x * kPairWarps);
 }
 
 // ---- big cells (block staged) and huge cells (tiles) -----------------------
@@ -2260,7 +2268,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_fused(Params pin, FusedArg
         small_pass<D, false, NARROW, false, true>(p, sa, sa + kSmallSlots, reinterpret_cast<uint2*>(sa + 2 * kSmallSlots),
                                             gw, nw);
         __syncthreads();
-        med_pass<D, false, NARROW, false, true>(p, smem_raw + warp * kMedWarpBytes);
+        med_pass<D, false, NARROW, false, true>(p, smem_raw + warp * kMedWarpBytes, gw, nw);
         __syncthreads();
         if (t < kPairThreads)  // (the block pass is laid out for kPairThreads threads)
             block_pass<D, false, NARROW, false, true, true>(p, *reinterpret_cast<BlockSmem*>(smem_raw), blk, nblk);
