@@ -835,7 +835,7 @@ constexpr uint32_t kMissShift = 29;
 constexpr uint32_t kWarpOut = 256;          // per-warp output buffer (pairs), small cells
 constexpr uint32_t kMedOut = 512;           // per-warp output buffer (pairs), medium cells: above the
                                             // typical output of one emission step, so it rarely spills
-constexpr uint32_t kSmallSlots = 32;        // per-warp staging, small cells
+constexpr uint32_t kSmallSlots = 64;        // per-warp staging, small cells (each cell twice in a row)
 constexpr uint32_t kMedSlots = kMedMax;     // per-warp staging, medium cells
 constexpr uint32_t kBlockSlots = kBigMax;   // per-block staging, big cells
 constexpr uint32_t kBlockOut = 2048;        // per-block output buffer (pairs)
@@ -1208,6 +1208,54 @@ __device__ __forceinline__ void row_unit(const Params& p, const Slots& s, uint32
     }
 }
 
+// Medium-cell staging. With coordinates < 2^29 a slot holds its box as the
+// six signed terms (-x1, x0, -y1, y0, -z1, z0) (then f and the index), and a
+// row box is taken as the partner terms (x0-1, -x1-1, y0-1, -y1-1, z0-1,
+// -z1-1). Each sum row_k + col_k is the gap between the two boxes along one
+// axis and side minus one (a.x0 - c.x1 - 1, c.x0 - a.x1 - 1, ...), so the
+// closed boxes overlap iff the largest of the six sums is negative: one add
+// and five add-max instructions per test, the result's sign bit the hit.
+// Wider coordinates keep the plain layout and comparisons.
+struct SepRow {
+    int t0, t1, t2, t3, t4, t5;
+};
+template <bool NARROW> struct MedRowT { using type = Box; };
+template <> struct MedRowT<true> { using type = SepRow; };
+
+template <bool NARROW>
+__device__ __forceinline__ void med_slot_put(const Slots& s, uint32_t i, const Box& x) {
+    if constexpr (NARROW) {
+        s.a[i] = make_uint4(0u - x.x1, x.x0, 0u - x.y1, x.y0);
+        s.b[i] = make_uint4(0u - x.z1, x.z0, x.f, x.id);
+    } else {
+        slot_put(s, i, x);
+    }
+}
+
+// the row form of a staged box (st: slot_get of its slot)
+template <bool NARROW>
+__device__ __forceinline__ typename MedRowT<NARROW>::type med_row(const Box& st) {
+    if constexpr (NARROW) {  // slot_get maps (-x1, x0, -y1, y0, -z1, z0) to (x0, x1, y0, y1, z0, z1)
+        return SepRow{(int)st.x1 - 1, (int)st.x0 - 1, (int)st.y1 - 1, (int)st.y0 - 1, (int)st.z1 - 1, (int)st.z0 - 1};
+    } else {
+        return st;
+    }
+}
+
+// bit 31 set iff row box r and column box (ca, cz) overlap
+template <int D>
+__device__ __forceinline__ uint32_t sep_hit(const SepRow& r, const uint4& ca, const uint2& cz) {
+    int m = r.t0 + (int)ca.x;
+    m = __viaddmax_s32(r.t1, (int)ca.y, m);
+    m = __viaddmax_s32(r.t2, (int)ca.z, m);
+    m = __viaddmax_s32(r.t3, (int)ca.w, m);
+    if (D == 3) {
+        m = __viaddmax_s32(r.t4, (int)cz.x, m);
+        m = __viaddmax_s32(r.t5, (int)cz.y, m);
+    }
+    return (uint32_t)m;
+}
+
 // ---- small cells ------------------------------------------------------------
 // lane group g (WG lanes) holds cell item*G+g of the class list, lane r its
 // box r; the circular half sweep runs inside the group.
@@ -1233,6 +1281,62 @@ __device__ __forceinline__ Box small_fetch(const Params& p, int list, uint64_t n
 template <int D, int WG, bool BIP, bool NARROW, bool REC>
 __device__ __forceinline__ void small_sweep(const Params& p, const Slots& s, WarpOut& o, const Box& me, uint32_t n,
                                             uint32_t lane, uint32_t g, uint32_t r, uint32_t gid) {
+    if constexpr (NARROW && !REC) {
+        // the medium-cell test: boxes staged as separation terms, one add and
+        // add-max instructions per test; the group's cell staged twice in a
+        // row, so partner r+d needs no wrap; the reference-cell and red/blue
+        // rules applied once per cell from ballots. Slot i: s.a[i] the x and y
+        // terms, then in s.b's space the z terms (8 bytes per slot, so a
+        // warp's loads take two wavefronts) and the box index.
+        const uint32_t gb = g * (2 * WG);
+        uint2* zz = reinterpret_cast<uint2*>(s.b);
+        uint32_t* ids = reinterpret_cast<uint32_t*>(s.b) + 2 * kSmallSlots;
+        if (r < n) {
+            const uint4 xa = make_uint4(0u - me.x1, me.x0, 0u - me.y1, me.y0);
+            s.a[gb + r] = xa;
+            s.a[gb + n + r] = xa;
+            if (D == 3) {
+                const uint2 zt = make_uint2(0u - me.z1, me.z0);
+                zz[gb + r] = zt;
+                zz[gb + n + r] = zt;
+            }
+            ids[gb + r] = me.id;
+            ids[gb + n + r] = me.id;
+        }
+        __syncwarp();
+        const uint32_t nelm = r < n ? (r < (n >> 1) ? (n >> 1) : ((n - 1) >> 1)) : 0u;
+        const uint32_t dlim = __reduce_max_sync(FULL_MASK, nelm);
+        // bit j: group lane j is a partner the rules exclude
+        const uint32_t sh = WG == 32 ? 0u : g * WG;
+        const uint32_t nm = n >= 32u ? FULL_MASK : ((1u << n) - 1u);
+        const uint32_t fa = me.f >> kMissShift;
+        const uint32_t m0 = (__ballot_sync(FULL_MASK, (fa & 1u) != 0u) >> sh) & nm;
+        const uint32_t m1 = (__ballot_sync(FULL_MASK, (fa & 2u) != 0u) >> sh) & nm;
+        const uint32_t m2 = (__ballot_sync(FULL_MASK, (fa & 4u) != 0u) >> sh) & nm;
+        uint32_t deny = ((fa & 1u) ? m0 : 0u) | ((fa & 2u) ? m1 : 0u) | ((fa & 4u) ? m2 : 0u);
+        if (BIP) {
+            const uint32_t red = (__ballot_sync(FULL_MASK, me.id < p.split) >> sh) & nm;
+            deny |= me.id < p.split ? red : (~red & nm);
+        }
+        // bit d: partner (r + d) mod n
+        uint32_t rot = 0;
+        if (r < n) rot = n >= 32u ? __funnelshift_r(deny, deny, r) : (((deny >> r) | (deny << (n - r))) & nm);
+        const SepRow row{(int)me.x0 - 1, -(int)me.x1 - 1, (int)me.y0 - 1, -(int)me.y1 - 1, (int)me.z0 - 1,
+                         -(int)me.z1 - 1};
+        uint32_t mask = 0;
+#pragma unroll
+        for (uint32_t d = 1; d <= WG / 2; d++) {
+            if (d > dlim) break;
+            const uint32_t i = gb + r + d;
+            const uint4 ca = s.a[i];
+            const uint2 cz = D == 3 ? zz[i] : make_uint2(0u, 0u);
+            mask |= (sep_hit<D>(row, ca, cz) >> 31) << d;
+        }
+        mask &= ~rot & ((2u << nelm) - 2u);
+        auto pid = [&](uint32_t d) { return ids[gb + r + d]; };
+        wemit<BIP>(p, o, mask, pid, 0u, pid, me.id);
+        return;
+    }
     slot_put(s, lane, me);
     __syncwarp();
     const uint32_t gb = g * WG;
@@ -1354,54 +1458,6 @@ __device__ __forceinline__ uint32_t miss_word(const Box& a, const uint4& ca, con
 }
 
 __device__ __forceinline__ uint32_t push_hit(uint32_t mask, uint32_t miss) { return __funnelshift_l(~miss, mask, 1); }
-
-// Medium-cell staging. With coordinates < 2^29 a slot holds its box as the
-// six signed terms (-x1, x0, -y1, y0, -z1, z0) (then f and the index), and a
-// row box is taken as the partner terms (x0-1, -x1-1, y0-1, -y1-1, z0-1,
-// -z1-1). Each sum row_k + col_k is the gap between the two boxes along one
-// axis and side minus one (a.x0 - c.x1 - 1, c.x0 - a.x1 - 1, ...), so the
-// closed boxes overlap iff the largest of the six sums is negative: one add
-// and five add-max instructions per test, the result's sign bit the hit.
-// Wider coordinates keep the plain layout and comparisons.
-struct SepRow {
-    int t0, t1, t2, t3, t4, t5;
-};
-template <bool NARROW> struct MedRowT { using type = Box; };
-template <> struct MedRowT<true> { using type = SepRow; };
-
-template <bool NARROW>
-__device__ __forceinline__ void med_slot_put(const Slots& s, uint32_t i, const Box& x) {
-    if constexpr (NARROW) {
-        s.a[i] = make_uint4(0u - x.x1, x.x0, 0u - x.y1, x.y0);
-        s.b[i] = make_uint4(0u - x.z1, x.z0, x.f, x.id);
-    } else {
-        slot_put(s, i, x);
-    }
-}
-
-// the row form of a staged box (st: slot_get of its slot)
-template <bool NARROW>
-__device__ __forceinline__ typename MedRowT<NARROW>::type med_row(const Box& st) {
-    if constexpr (NARROW) {  // slot_get maps (-x1, x0, -y1, y0, -z1, z0) to (x0, x1, y0, y1, z0, z1)
-        return SepRow{(int)st.x1 - 1, (int)st.x0 - 1, (int)st.y1 - 1, (int)st.y0 - 1, (int)st.z1 - 1, (int)st.z0 - 1};
-    } else {
-        return st;
-    }
-}
-
-// bit 31 set iff row box r and column box (ca, cz) overlap
-template <int D>
-__device__ __forceinline__ uint32_t sep_hit(const SepRow& r, const uint4& ca, const uint2& cz) {
-    int m = r.t0 + (int)ca.x;
-    m = __viaddmax_s32(r.t1, (int)ca.y, m);
-    m = __viaddmax_s32(r.t2, (int)ca.z, m);
-    m = __viaddmax_s32(r.t3, (int)ca.w, m);
-    if (D == 3) {
-        m = __viaddmax_s32(r.t4, (int)cz.x, m);
-        m = __viaddmax_s32(r.t5, (int)cz.y, m);
-    }
-    return (uint32_t)m;
-}
 
 template <int D, bool NARROW, class Row>
 __device__ __forceinline__ uint32_t test_slot(const Slots& s, const Row& me, uint32_t mask, uint32_t i) {
@@ -2004,6 +2060,7 @@ constexpr uint32_t kFusedLocalCells = 8192;  // grids of up to 8192 cells: 128-c
 constexpr uint32_t kGridWaitLimit = 1u << 20;  // polls of 64 ns or more: the wait ends after a second at most
 constexpr uint32_t kSmallWarpBytes = 2 * kSmallSlots * sizeof(uint4) + kWarpOut * sizeof(uint2);
 static_assert(kFusedChunks % kFusedThreads == 0, "chunk prefixes per thread");
+static_assert(kSmallSlots * sizeof(uint2) + kSmallSlots * sizeof(uint32_t) <= kSmallSlots * sizeof(uint4), "small-cell z terms and indices in the b array");
 
 // barrier number k of this launch (k counts the barriers passed so far)
 __device__ __forceinline__ bool grid_barrier(const FusedArgs& a, uint32_t k) {
