@@ -1222,14 +1222,42 @@ struct SepRow {
 template <bool NARROW> struct MedRowT { using type = Box; };
 template <> struct MedRowT<true> { using type = SepRow; };
 
+// (with narrow coordinates the b array's space holds the z terms,
+// uint2[kMedSlots], then {f, id}, uint2[kMedSlots]: 8-byte loads of
+// consecutive slots take two wavefronts a warp, not four)
+__device__ __forceinline__ uint2* med_z(const Slots& s) { return reinterpret_cast<uint2*>(s.b); }
+__device__ __forceinline__ uint2* med_fi(const Slots& s) { return reinterpret_cast<uint2*>(s.b) + kMedSlots; }
+
 template <bool NARROW>
 __device__ __forceinline__ void med_slot_put(const Slots& s, uint32_t i, const Box& x) {
     if constexpr (NARROW) {
         s.a[i] = make_uint4(0u - x.x1, x.x0, 0u - x.y1, x.y0);
-        s.b[i] = make_uint4(0u - x.z1, x.z0, x.f, x.id);
+        med_z(s)[i] = make_uint2(0u - x.z1, x.z0);
+        med_fi(s)[i] = make_uint2(x.f, x.id);
     } else {
         slot_put(s, i, x);
     }
+}
+
+// a staged medium-cell box in slot_get's form
+template <bool NARROW>
+__device__ __forceinline__ Box med_slot_get(const Slots& s, uint32_t i) {
+    if constexpr (NARROW) {
+        const uint4 a = s.a[i];
+        const uint2 z = med_z(s)[i], fi = med_fi(s)[i];
+        Box x;
+        x.x0 = a.x; x.x1 = a.y; x.y0 = a.z; x.y1 = a.w;
+        x.z0 = z.x; x.z1 = z.y; x.f = fi.x; x.id = fi.y;
+        return x;
+    } else {
+        return slot_get(s, i);
+    }
+}
+
+template <bool NARROW>
+__device__ __forceinline__ uint32_t med_slot_id(const Slots& s, uint32_t i) {
+    if constexpr (NARROW) return med_fi(s)[i].y;
+    else return slot_id(s, i);
 }
 
 // the row form of a staged box (st: slot_get of its slot)
@@ -1424,13 +1452,22 @@ __global__ void __launch_bounds__(kPairThreads, 5) k_pairs_small(Params p) {
 // mask with one funnel shift (mask = mask << 1 | hit).
 
 // columns [c0, c0 + ncol) of the staged cell that row box `me` may pair with
-template <bool BIP>
+template <bool BIP, bool NARROW>
 __device__ __forceinline__ uint32_t tile_allow(const Params& p, const Slots& s, uint32_t c0, uint32_t ncol,
                                                const Box& me) {
     const uint32_t lane = lane_id();
     const bool v = lane < ncol;
-    const uint4 b = s.b[c0 + (v ? lane : 0u)];
-    const uint32_t f = v ? b.z >> kMissShift : 0u;
+    uint32_t bf, bid;
+    if constexpr (NARROW) {
+        const uint2 fi = med_fi(s)[c0 + (v ? lane : 0u)];
+        bf = fi.x;
+        bid = fi.y;
+    } else {
+        const uint4 b = s.b[c0 + (v ? lane : 0u)];
+        bf = b.z;
+        bid = b.w;
+    }
+    const uint32_t f = v ? bf >> kMissShift : 0u;
     const uint32_t vm = __ballot_sync(FULL_MASK, v);
     const uint32_t m0 = __ballot_sync(FULL_MASK, (f & 1u) != 0u);
     const uint32_t m1 = __ballot_sync(FULL_MASK, (f & 2u) != 0u);
@@ -1438,7 +1475,7 @@ __device__ __forceinline__ uint32_t tile_allow(const Params& p, const Slots& s, 
     const uint32_t fa = me.f >> kMissShift;
     uint32_t allow = vm & ~(((fa & 1u) ? m0 : 0u) | ((fa & 2u) ? m1 : 0u) | ((fa & 4u) ? m2 : 0u));
     if (BIP) {
-        const uint32_t red = __ballot_sync(FULL_MASK, v && b.w < p.split);
+        const uint32_t red = __ballot_sync(FULL_MASK, v && bid < p.split);
         allow &= (me.id < p.split) ? ~red : red;
     }
     return allow;
@@ -1462,7 +1499,7 @@ __device__ __forceinline__ uint32_t push_hit(uint32_t mask, uint32_t miss) { ret
 template <int D, bool NARROW, class Row>
 __device__ __forceinline__ uint32_t test_slot(const Slots& s, const Row& me, uint32_t mask, uint32_t i) {
     const uint4 ca = s.a[i];
-    const uint2 cz = D == 3 ? *reinterpret_cast<const uint2*>(&s.b[i]) : make_uint2(0u, 0u);
+    const uint2 cz = D == 3 ? (NARROW ? med_z(s)[i] : *reinterpret_cast<const uint2*>(&s.b[i])) : make_uint2(0u, 0u);
     if constexpr (NARROW) return __funnelshift_l(sep_hit<D>(me, ca, cz), mask, 1);
     else return push_hit(mask, miss_word<D, false>(me, ca, cz));
 }
@@ -1555,28 +1592,28 @@ __device__ __forceinline__ void med_pass(const Params& p, unsigned char* wsm, ui
         __syncwarp();
         for (uint32_t r = 0; r < R; r++) {
             const uint32_t rows = min(32u, n - 32 * r), rb = 32 * r;
-            const Box me = slot_get(s, rb + lane);  // lanes >= rows hold a padding box, masked below
+            const Box me = med_slot_get<NARROW>(s, rb + lane);  // lanes >= rows hold a padding box, masked below
             const auto row = med_row<NARROW>(me);
             const uint32_t l = lane < rows ? lane : 0u;
             const uint32_t dm = sweep_diag2<D, NARROW>(s, row, l, rb, rows) &
-                                diag_allow(tile_allow<BIP>(p, s, rb, rows, me), lane, rows);
+                                diag_allow(tile_allow<BIP, NARROW>(p, s, rb, rows, me), lane, rows);
             const uint32_t dmax = rows >> 1;
             auto pdiag = [&](uint32_t k) {
                 uint32_t pr = l + dmax - k;
                 if (pr >= rows) pr -= rows;
-                return slot_id(s, rb + pr);
+                return med_slot_id<NARROW>(s, rb + pr);
             };
             uint32_t pend = dm;  // the diagonal's hits wait for the first column tile
             bool have = true;
             for (uint32_t x = r + 1; x < R; x++) {
                 const uint32_t c0 = 32 * x, ncol = min(32u, n - c0);
-                uint32_t allow = tile_allow<BIP>(p, s, c0, ncol, me);
+                uint32_t allow = tile_allow<BIP, NARROW>(p, s, c0, ncol, me);
                 if (lane >= rows) allow = 0u;
                 uint32_t mc = 0;
                 const uint32_t cnt = (ncol + 7) & ~7u;
                 if (__any_sync(FULL_MASK, allow != 0u))
                     mc = sweep_tile<D, NARROW>(s, row, c0, cnt) & (__brev(allow) >> (32u - cnt));
-                auto pcol = [&](uint32_t k) { return slot_id(s, c0 + cnt - 1 - k); };
+                auto pcol = [&](uint32_t k) { return med_slot_id<NARROW>(s, c0 + cnt - 1 - k); };
                 if constexpr (REC) {
                     auto lcol = [&](uint32_t k) { return c0 + cnt - 1 - k; };
                     auto ldiag = [&](uint32_t k) {
@@ -2060,6 +2097,7 @@ constexpr uint32_t kFusedLocalCells = 8192;  // grids of up to 8192 cells: 128-c
 constexpr uint32_t kGridWaitLimit = 1u << 20;  // polls of 64 ns or more: the wait ends after a second at most
 constexpr uint32_t kSmallWarpBytes = 2 * kSmallSlots * sizeof(uint4) + kWarpOut * sizeof(uint2);
 static_assert(kFusedChunks % kFusedThreads == 0, "chunk prefixes per thread");
+static_assert(2 * kMedSlots * sizeof(uint2) <= kMedSlots * sizeof(uint4), "medium-cell z terms and {f, id} in the b array");
 static_assert(kSmallSlots * sizeof(uint2) + kSmallSlots * sizeof(uint32_t) <= kSmallSlots * sizeof(uint4), "small-cell z terms and indices in the b array");
 
 // barrier number k of this launch (k counts the barriers passed so far)
