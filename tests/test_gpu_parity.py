@@ -276,6 +276,33 @@ def test_output_capacity_growth(engine):
     assert engine.self_intersect(b, 1000) == 3000 * 2999 // 2
 
 
+def test_medium_cells_rerun_after_pair_overflow():
+    """A fresh context on the multi-launch pipeline: 25 cells of 80 boxes
+    that all overlap (medium cells) give 79 000 pairs, more than the first
+    pair buffer holds, so the pair kernels run again on the same grid; the
+    medium-cell pass takes its cells from a counter, which the rerun must
+    start from zero again."""
+    from pbig_gb300 import Engine
+    rng = np.random.default_rng(7)
+    rows = []
+    for g in range(25):
+        lo = np.array([(g % 5) * 2048, (g // 5) * 2048, 4096]) + 10
+        for _ in range(80):
+            a = lo + rng.integers(0, 8, size=3)
+            b = a + rng.integers(8, 16, size=3)
+            rows.append([a[0], b[0], a[1], b[1], a[2], b[2], 0])
+    boxes = np.asarray(rows, dtype=np.uint32)
+    boxes[:, 6] = np.arange(len(boxes))
+    want = O.brute_pairs(boxes)
+    assert len(want) == 25 * 80 * 79 // 2
+    with Engine(0) as e:
+        e.set_one_launch(False)
+        for _ in range(2):
+            assert e.self_intersect(boxes, 1 << 16, cell_shift=10) == len(want)
+            assert e.stats()["max_cell"] == 80
+            assert np.array_equal(canon(e.pairs()), want)
+
+
 @pytest.mark.parametrize("kind", ["counting", "recording"])
 def test_legacy_pbig_api_client(tmp_path, kind):
     """A pbig.h client (pbig_init / pbig_check / pbig_finalize, report
